@@ -1,0 +1,174 @@
+"""ctypes binding of libcgx.so (the C ABI declared in include/cgx.h).
+
+The library is loaded from this package directory. There is no fallback:
+if libcgx.so is missing or fails to load, every call raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcgx.so")
+
+CGX_OK = 0
+CGX_ERR_INVALID_ARG = 1
+CGX_ERR_CUDA = 2
+CGX_ERR_OUT_OF_BOUNDS = 3
+CGX_ERR_TIMEOUT = 4
+CGX_ERR_NOT_SUPPORTED = 5
+CGX_ERR_NO_MEMORY = 6
+
+CGX_F32 = 0
+CGX_F64 = 1
+CGX_NODE = 0
+CGX_CELL = 1
+CGX_PLAIN_FP64 = 0
+CGX_FP32_COMPENSATED = 1
+
+CGX_FLAG_SKIP_HALO = 1
+CGX_FLAG_CHECK_BOUNDS = 2
+
+# Every exported symbol declared in include/cgx.h.
+EXPORTS = (
+    "cgx_create", "cgx_destroy", "cgx_last_error", "cgx_version",
+    "cgx_p2g", "cgx_g2p", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
+    "cgx_cartesian_num_bins", "cgx_linked_cell_build", "cgx_bin_by_key", "cgx_permute",
+    "cgx_tiling_init", "cgx_tiling_num_offsets", "cgx_sort_tiles",
+)
+
+
+class CgxMesh(ctypes.Structure):
+    _fields_ = [
+        ("ghost_low", ctypes.c_double * 3),
+        ("cell_size", ctypes.c_double * 3),
+        ("owned_cells", ctypes.c_int32 * 3),
+        ("halo_width", ctypes.c_int32),
+        ("periodic", ctypes.c_int32 * 3),
+        ("entity", ctypes.c_int32),
+    ]
+
+
+class CgxField(ctypes.Structure):
+    _fields_ = [
+        ("data", ctypes.c_void_p),
+        ("dtype", ctypes.c_int32),
+        ("vector_length", ctypes.c_int32),
+        ("soa_stride", ctypes.c_int64),
+        ("comp_stride", ctypes.c_int64),
+    ]
+
+
+class CgxArray(ctypes.Structure):
+    _fields_ = [
+        ("data", ctypes.c_void_p),
+        ("dtype", ctypes.c_int32),
+        ("dofs", ctypes.c_int32),
+    ]
+
+
+class CgxOp(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("multiplier", ctypes.c_double),
+        ("x", CgxField),
+        ("array", CgxArray),
+    ]
+
+
+class CgxTiling(ctypes.Structure):
+    _fields_ = [
+        ("tile", ctypes.c_int32 * 3),
+        ("num_tiles", ctypes.c_int32 * 3),
+        ("spline_order", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("tile_offsets", ctypes.c_void_p),
+    ]
+
+
+class CgxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"cgx error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load libcgx.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() (or python cabana_gb300/build.py)")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    L.cgx_create.argtypes = [P(vp)]
+    L.cgx_destroy.argtypes = [vp]
+    L.cgx_last_error.restype = ctypes.c_char_p
+    L.cgx_version.restype = ctypes.c_char_p
+    interp = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, ctypes.c_int, P(CgxOp), ctypes.c_int, ctypes.c_int,
+              P(CgxTiling), ctypes.c_uint, vp]
+    L.cgx_p2g.argtypes = interp
+    L.cgx_g2p.argtypes = interp
+    L.cgx_halo_scatter_sum.argtypes = [P(CgxMesh), P(CgxArray), vp]
+    L.cgx_halo_gather.argtypes = [P(CgxMesh), P(CgxArray), vp]
+    L.cgx_array_assign.argtypes = [P(CgxMesh), P(CgxArray), ctypes.c_double, vp]
+    d3 = ctypes.c_double * 3
+    L.cgx_cartesian_num_bins.argtypes = [d3, d3, d3, ctypes.c_int32 * 3]
+    L.cgx_linked_cell_build.argtypes = [vp, P(CgxField), ctypes.c_int64, ctypes.c_int64, d3, d3, d3, vp, vp, vp, vp]
+    L.cgx_bin_by_key.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, vp, vp, vp, vp]
+    L.cgx_permute.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int64, P(CgxField), P(ctypes.c_int32), ctypes.c_int, vp]
+    L.cgx_tiling_init.argtypes = [P(CgxMesh), ctypes.c_int, ctypes.c_int32 * 3, P(CgxTiling)]
+    L.cgx_tiling_num_offsets.argtypes = [P(CgxTiling)]
+    L.cgx_tiling_num_offsets.restype = ctypes.c_int64
+    L.cgx_sort_tiles.argtypes = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, P(CgxTiling), vp, vp]
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != CGX_OK:
+        raise CgxError(status, lib().cgx_last_error().decode())
+    return status
+
+
+def make_mesh(params):
+    """CgxMesh from a cabana_gb300.mesh.MeshParams."""
+    m = CgxMesh()
+    for d in range(3):
+        m.ghost_low[d] = params.ghost_low[d]
+        m.cell_size[d] = params.cell_size[d]
+        m.owned_cells[d] = params.owned_cells[d]
+        m.periodic[d] = params.periodic[d]
+    m.halo_width = params.halo_width
+    m.entity = params.entity
+    return m
+
+
+class Handle:
+    """Owns one cgx_handle (workspace, error flags)."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().cgx_create(ctypes.byref(h)))
+        self.ptr = h
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().cgx_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+_default = None
+
+
+def default_handle():
+    global _default
+    if _default is None:
+        _default = Handle()
+    return _default

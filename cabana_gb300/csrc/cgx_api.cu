@@ -1,0 +1,590 @@
+// C ABI of libcgx: argument checks, workspace, dispatch to the kernels.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "cgx_kernels.cuh"
+
+using namespace cgx;
+
+struct cgx_context {
+    int device = 0;
+    int sms = 0;
+    void* ws = nullptr;  // grow-only workspace
+    size_t ws_bytes = 0;
+    int* flags = nullptr;  // [0] error flag, [1] work counter, [2..3] work count (int64)
+    WorkItem* work = nullptr;
+    size_t work_cap = 0;
+    int64_t* work_prefix = nullptr;
+    size_t prefix_cap = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+cgx_status fail(cgx_status code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+cgx_status cuda_fail(cudaError_t e, const char* where) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return CGX_ERR_CUDA;
+}
+
+#define CGX_CUDA(call)                                  \
+    do {                                                \
+        cudaError_t _e = (call);                        \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+    } while (0)
+
+cgx_status ensure_ws(cgx_context* h, size_t bytes) {
+    if (bytes <= h->ws_bytes) return CGX_OK;
+    if (h->ws) cudaFree(h->ws);
+    h->ws = nullptr;
+    h->ws_bytes = 0;
+    size_t want = bytes + bytes / 8 + (1 << 20);
+    cudaError_t e = cudaMalloc(&h->ws, want);
+    if (e != cudaSuccess) return fail(CGX_ERR_NO_MEMORY, std::string("workspace allocation failed: ") + cudaGetErrorString(e));
+    h->ws_bytes = want;
+    return CGX_OK;
+}
+
+bool valid_dtype(int t) { return t == CGX_F32 || t == CGX_F64; }
+
+cgx_status check_mesh(const cgx_mesh* m) {
+    if (!m) return fail(CGX_ERR_INVALID_ARG, "mesh is NULL");
+    for (int d = 0; d < 3; ++d) {
+        if (!(m->cell_size[d] > 0.0)) return fail(CGX_ERR_INVALID_ARG, "cell_size must be positive");
+        if (m->owned_cells[d] < 1) return fail(CGX_ERR_INVALID_ARG, "owned_cells must be >= 1");
+    }
+    if (m->halo_width < 0) return fail(CGX_ERR_INVALID_ARG, "halo_width must be >= 0");
+    if (m->entity != CGX_NODE && m->entity != CGX_CELL) return fail(CGX_ERR_INVALID_ARG, "entity must be CGX_NODE or CGX_CELL");
+    for (int d = 0; d < 3; ++d) {
+        if (m->periodic[d] && m->halo_width >= m->owned_cells[d])
+            return fail(CGX_ERR_INVALID_ARG, "periodic halo wider than the owned cells");
+    }
+    return CGX_OK;
+}
+
+cgx_status check_field(const cgx_field* f, const char* what) {
+    if (!f) return fail(CGX_ERR_INVALID_ARG, std::string(what) + " is NULL");
+    if (!f->data) return fail(CGX_ERR_INVALID_ARG, std::string(what) + ".data is NULL");
+    if (!valid_dtype(f->dtype)) return fail(CGX_ERR_INVALID_ARG, std::string(what) + ": dtype must be CGX_F32 or CGX_F64");
+    const int vl = f->vector_length;
+    if (vl < 1 || (vl & (vl - 1))) return fail(CGX_ERR_INVALID_ARG, std::string(what) + ": vector_length must be a power of two");
+    return CGX_OK;
+}
+
+DField to_dfield(const cgx_field& f) {
+    DField d;
+    d.data = reinterpret_cast<char*>(f.data);
+    d.dtype = f.dtype;
+    d.log2vl = log2_int(f.vector_length);
+    d.soa_stride = f.soa_stride;
+    d.comp_stride = f.comp_stride;
+    return d;
+}
+
+// LocalMesh::coordinates(Entity, index) (grid/src/Cabana_Grid_LocalMesh.hpp:
+// 180-200) and the dx / rdx of evaluateSpline (Splines.hpp:1293-1311).
+DMesh to_dmesh(const cgx_mesh& m) {
+    DMesh d;
+    for (int a = 0; a < 3; ++a) {
+        double lo, hi;
+        if (m.entity == CGX_CELL) {
+            lo = m.ghost_low[a] + (double(0) + double(0.5)) * m.cell_size[a];
+            hi = m.ghost_low[a] + (double(1) + double(0.5)) * m.cell_size[a];
+        } else {
+            lo = m.ghost_low[a] + double(0) * m.cell_size[a];
+            hi = m.ghost_low[a] + double(1) * m.cell_size[a];
+        }
+        const double dx = hi - lo;
+        d.low[a] = lo;
+        d.rdx[a] = 1.0 / dx;
+        d.rdx_f[a] = float(d.rdx[a]);
+        d.ext[a] = m.owned_cells[a] + 2 * m.halo_width + (m.entity == CGX_NODE ? 1 : 0);
+    }
+    return d;
+}
+
+int p2g_comps(int kind) {
+    switch (kind) {
+        case CGX_SCALAR_VALUE_P2G: case CGX_SCALAR_GRADIENT_P2G: return 1;
+        case CGX_VECTOR_VALUE_P2G: case CGX_VECTOR_DIVERGENCE_P2G: return 3;
+        case CGX_TENSOR_DIVERGENCE_P2G: return 9;
+    }
+    return -1;
+}
+int p2g_dofs(int kind) {
+    switch (kind) {
+        case CGX_SCALAR_VALUE_P2G: case CGX_VECTOR_DIVERGENCE_P2G: return 1;
+        case CGX_VECTOR_VALUE_P2G: case CGX_SCALAR_GRADIENT_P2G: case CGX_TENSOR_DIVERGENCE_P2G: return 3;
+    }
+    return -1;
+}
+int g2p_comps(int kind) {
+    switch (kind) {
+        case CGX_SCALAR_VALUE_G2P: case CGX_VECTOR_DIVERGENCE_G2P: return 1;
+        case CGX_VECTOR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 3;
+        case CGX_VECTOR_GRADIENT_G2P: return 9;
+    }
+    return -1;
+}
+int g2p_dofs(int kind) {
+    switch (kind) {
+        case CGX_SCALAR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 1;
+        case CGX_VECTOR_VALUE_G2P: case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_DIVERGENCE_G2P: return 3;
+    }
+    return -1;
+}
+
+bool any_periodic(const cgx_mesh& m) { return m.periodic[0] || m.periodic[1] || m.periodic[2]; }
+
+HaloParams to_halo(const cgx_mesh& m, const cgx_array& a) {
+    HaloParams h;
+    h.data = reinterpret_cast<char*>(a.data);
+    h.dtype = a.dtype;
+    h.dofs = a.dofs;
+    for (int d = 0; d < 3; ++d) {
+        h.ext[d] = m.owned_cells[d] + 2 * m.halo_width + (m.entity == CGX_NODE ? 1 : 0);
+        h.owned_cells[d] = m.owned_cells[d];
+        h.periodic[d] = m.periodic[d] ? 1 : 0;
+    }
+    h.halo_width = m.halo_width;
+    h.node_extra = m.entity == CGX_NODE ? 1 : 0;
+    return h;
+}
+
+cgx_status check_ops(const cgx_op* ops, int n_ops, bool p2g, bool have_points) {
+    if (!ops || n_ops < 1 || n_ops > kMaxOps) return fail(CGX_ERR_INVALID_ARG, "n_ops must be in [1, 8]");
+    for (int o = 0; o < n_ops; ++o) {
+        const cgx_op& op = ops[o];
+        const int comps = p2g ? p2g_comps(op.kind) : g2p_comps(op.kind);
+        const int dofs = p2g ? p2g_dofs(op.kind) : g2p_dofs(op.kind);
+        if (comps < 0) return fail(CGX_ERR_INVALID_ARG, "unknown operator kind");
+        if (have_points) {
+            cgx_status s = check_field(&op.x, "op.x");
+            if (s) return s;
+        }
+        if (!op.array.data) return fail(CGX_ERR_INVALID_ARG, "op.array.data is NULL");
+        if (!valid_dtype(op.array.dtype)) return fail(CGX_ERR_INVALID_ARG, "op.array.dtype must be CGX_F32 or CGX_F64");
+        if (op.array.dofs < dofs) return fail(CGX_ERR_INVALID_ARG, "array has fewer dofs than the operator writes/reads");
+    }
+    return CGX_OK;
+}
+
+cgx_status finish_check(cgx_context* h, unsigned flags, cudaStream_t st) {
+    if (!(flags & CGX_FLAG_CHECK_BOUNDS)) return CGX_OK;
+    int host_flag = 0;
+    CGX_CUDA(cudaMemcpyAsync(&host_flag, h->flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CGX_CUDA(cudaStreamSynchronize(st));
+    if (host_flag & (1 << CGX_ERR_OUT_OF_BOUNDS))
+        return fail(CGX_ERR_OUT_OF_BOUNDS, "a point's stencil left the ghosted index space; it was skipped");
+    if (host_flag & (1 << CGX_ERR_INVALID_ARG)) return fail(CGX_ERR_INVALID_ARG, "a key was outside [0, nbin)");
+    return CGX_OK;
+}
+
+cgx_status halo_all(const cgx_mesh& m, const cgx_op* ops, int n_ops, bool scatter, int sms, cudaStream_t st) {
+    if (!any_periodic(m)) return CGX_OK;
+    for (int o = 0; o < n_ops; ++o) {
+        bool seen = false;
+        for (int q = 0; q < o; ++q) seen |= ops[q].array.data == ops[o].array.data;
+        if (seen) continue;
+        CGX_CUDA(launch_halo(to_halo(m, ops[o].array), scatter, sms, st));
+    }
+    return CGX_OK;
+}
+
+constexpr int64_t kChunk = 2048;
+
+cgx_status build_work(cgx_context* h, const cgx_tiling& t, int64_t num_point, cudaStream_t st) {
+    const int64_t nt = int64_t(t.num_tiles[0]) * t.num_tiles[1] * t.num_tiles[2];
+    const size_t cap = size_t(nt + num_point / kChunk + 1);
+    if (cap > h->work_cap) {
+        if (h->work) cudaFree(h->work);
+        h->work = nullptr;
+        h->work_cap = 0;
+        CGX_CUDA(cudaMalloc(&h->work, cap * sizeof(WorkItem)));
+        h->work_cap = cap;
+    }
+    if (size_t(nt) > h->prefix_cap) {
+        if (h->work_prefix) cudaFree(h->work_prefix);
+        h->work_prefix = nullptr;
+        h->prefix_cap = 0;
+        CGX_CUDA(cudaMalloc(&h->work_prefix, size_t(nt) * sizeof(int64_t)));
+        h->prefix_cap = size_t(nt);
+    }
+    cgx_status s = ensure_ws(h, size_t(nt) * 4 + 512 + scan_scratch_bytes(nt));
+    if (s) return s;
+    CGX_CUDA(build_work_items(t.tile_offsets, nt, kChunk, h->work_prefix, h->work,
+                              reinterpret_cast<int64_t*>(h->flags + 2), h->ws, st, h->sms));
+    return CGX_OK;
+}
+
+cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point,
+                       int spline_order, const cgx_op* ops, int n_ops, int precision, const cgx_tiling* tiling,
+                       unsigned flags, void* stream, bool p2g) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    if (num_point < 0) return fail(CGX_ERR_INVALID_ARG, "num_point must be >= 0");
+    if (num_point > 0) {
+        s = check_field(points, "points");
+        if (s) return s;
+        if (points->dtype != CGX_F64) return fail(CGX_ERR_INVALID_ARG, "point coordinates must be double (CGX_F64)");
+    }
+    if (spline_order < 0 || spline_order > 6) return fail(CGX_ERR_NOT_SUPPORTED, "spline order must be in [0, 6]");
+    if (precision != CGX_PLAIN_FP64 && precision != CGX_FP32_COMPENSATED)
+        return fail(CGX_ERR_INVALID_ARG, "unknown precision");
+    s = check_ops(ops, n_ops, p2g, num_point > 0);
+    if (s) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (flags & CGX_FLAG_CHECK_BOUNDS) CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
+
+    const DMesh dm = to_dmesh(*mesh);
+    if (!p2g && !(flags & CGX_FLAG_SKIP_HALO)) {
+        s = halo_all(*mesh, ops, n_ops, false, h->sms, st);
+        if (s) return s;
+    }
+
+    bool tiled = num_point > 0 && tiling && precision == CGX_FP32_COMPENSATED && tiling->tile_offsets &&
+                 tiling->spline_order == spline_order && spline_order >= 1 && spline_order <= 3;
+    if (tiled) {
+        TiledParams prm;
+        std::memset(&prm, 0, sizeof(prm));
+        prm.mesh = dm;
+        prm.points = to_dfield(*points);
+        prm.num_point = num_point;
+        prm.n_ops = n_ops;
+        const int nk = spline_order + 1;
+        for (int d = 0; d < 3; ++d) {
+            prm.tile[d] = tiling->tile[d];
+            prm.num_tiles[d] = tiling->num_tiles[d];
+            prm.box[d] = tiling->tile[d] + nk - 1;
+        }
+        prm.box_nodes = prm.box[0] * prm.box[1] * prm.box[2];
+        int n_arrays = 0;
+        int offset = 0;
+        for (int o = 0; o < n_ops; ++o) {
+            int slot = -1;
+            for (int a = 0; a < n_arrays; ++a)
+                if (prm.arrays[a].a.data == ops[o].array.data) slot = a;
+            if (slot < 0) {
+                slot = n_arrays++;
+                prm.arrays[slot].a.data = reinterpret_cast<char*>(ops[o].array.data);
+                prm.arrays[slot].a.dtype = ops[o].array.dtype;
+                prm.arrays[slot].a.dofs = ops[o].array.dofs;
+                prm.arrays[slot].smem_offset = offset;
+                offset += prm.box_nodes * ops[o].array.dofs * (p2g ? 2 : 1);
+            }
+            prm.ops[o].kind = ops[o].kind;
+            prm.ops[o].slot = slot;
+            prm.ops[o].mult = ops[o].multiplier;
+            prm.ops[o].x = to_dfield(ops[o].x);
+            prm.ops[o].a = prm.arrays[slot].a;
+        }
+        prm.n_arrays = n_arrays;
+        prm.smem_floats = offset;
+        const size_t smem = size_t(offset) * sizeof(float);
+        if (smem > 200 * 1024) tiled = false;  // box too large: use the point kernel
+        if (tiled) {
+            s = build_work(h, *tiling, num_point, st);
+            if (s) return s;
+            prm.work = h->work;
+            prm.work_count = reinterpret_cast<const int64_t*>(h->flags + 2);
+            prm.work_counter = h->flags + 1;
+            prm.error_flag = h->flags;
+            CGX_CUDA(cudaMemsetAsync(h->flags + 1, 0, sizeof(int), st));
+            CGX_CUDA(launch_tiled(prm, spline_order, p2g, h->sms, smem, st));
+        }
+    }
+    if (!tiled && num_point > 0) {
+        PointParams prm;
+        std::memset(&prm, 0, sizeof(prm));
+        prm.mesh = dm;
+        prm.points = to_dfield(*points);
+        prm.num_point = num_point;
+        prm.n_ops = n_ops;
+        prm.error_flag = h->flags;
+        for (int o = 0; o < n_ops; ++o) {
+            prm.ops[o].kind = ops[o].kind;
+            prm.ops[o].slot = o;
+            prm.ops[o].mult = ops[o].multiplier;
+            prm.ops[o].x = to_dfield(ops[o].x);
+            prm.ops[o].a.data = reinterpret_cast<char*>(ops[o].array.data);
+            prm.ops[o].a.dtype = ops[o].array.dtype;
+            prm.ops[o].a.dofs = ops[o].array.dofs;
+        }
+        CGX_CUDA(launch_points(prm, spline_order, p2g, precision == CGX_PLAIN_FP64, h->sms, st));
+    }
+    if (p2g && !(flags & CGX_FLAG_SKIP_HALO)) {
+        s = halo_all(*mesh, ops, n_ops, true, h->sms, st);
+        if (s) return s;
+    }
+    return finish_check(h, flags, st);
+}
+
+int key_bits_for(int64_t nbin) {
+    int b = 0;
+    while ((int64_t(1) << b) < nbin) ++b;
+    return b;
+}
+
+char* align256(char* p) { return reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 255) / 256 * 256); }
+
+}  // namespace
+
+extern "C" {
+
+cgx_status cgx_create(cgx_handle* out) {
+    if (!out) return fail(CGX_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    cgx_context* h = new cgx_context();
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (e == cudaSuccess) e = cudaMalloc(&h->flags, 64);
+    if (e == cudaSuccess) e = cudaMemset(h->flags, 0, 64);
+    if (e != cudaSuccess) {
+        if (h->flags) cudaFree(h->flags);
+        delete h;
+        return cuda_fail(e, "cgx_create");
+    }
+    *out = h;
+    return CGX_OK;
+}
+
+cgx_status cgx_destroy(cgx_handle h) {
+    if (!h) return CGX_OK;
+    if (h->ws) cudaFree(h->ws);
+    if (h->flags) cudaFree(h->flags);
+    if (h->work) cudaFree(h->work);
+    if (h->work_prefix) cudaFree(h->work_prefix);
+    delete h;
+    return CGX_OK;
+}
+
+const char* cgx_last_error(void) { return g_last_error.c_str(); }
+
+const char* cgx_version(void) { return "cgx 0.1 (sm_103a)"; }
+
+cgx_status cgx_p2g(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point, int spline_order,
+                   const cgx_op* ops, int n_ops, int precision, const cgx_tiling* tiling, unsigned flags,
+                   void* stream) {
+    return interpolate(h, mesh, points, num_point, spline_order, ops, n_ops, precision, tiling, flags, stream, true);
+}
+
+cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point, int spline_order,
+                   const cgx_op* ops, int n_ops, int precision, const cgx_tiling* tiling, unsigned flags,
+                   void* stream) {
+    return interpolate(h, mesh, points, num_point, spline_order, ops, n_ops, precision, tiling, flags, stream, false);
+}
+
+cgx_status cgx_halo_scatter_sum(const cgx_mesh* mesh, const cgx_array* array, void* stream) {
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    if (!array || !array->data || !valid_dtype(array->dtype) || array->dofs < 1)
+        return fail(CGX_ERR_INVALID_ARG, "bad array");
+    if (!any_periodic(*mesh)) return CGX_OK;
+    int dev = 0, sms = 0;
+    CGX_CUDA(cudaGetDevice(&dev));
+    CGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CGX_CUDA(launch_halo(to_halo(*mesh, *array), true, sms, reinterpret_cast<cudaStream_t>(stream)));
+    return CGX_OK;
+}
+
+cgx_status cgx_halo_gather(const cgx_mesh* mesh, const cgx_array* array, void* stream) {
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    if (!array || !array->data || !valid_dtype(array->dtype) || array->dofs < 1)
+        return fail(CGX_ERR_INVALID_ARG, "bad array");
+    if (!any_periodic(*mesh)) return CGX_OK;
+    int dev = 0, sms = 0;
+    CGX_CUDA(cudaGetDevice(&dev));
+    CGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CGX_CUDA(launch_halo(to_halo(*mesh, *array), false, sms, reinterpret_cast<cudaStream_t>(stream)));
+    return CGX_OK;
+}
+
+cgx_status cgx_array_assign(const cgx_mesh* mesh, const cgx_array* array, double value, void* stream) {
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    if (!array || !array->data || !valid_dtype(array->dtype) || array->dofs < 1)
+        return fail(CGX_ERR_INVALID_ARG, "bad array");
+    const DMesh dm = to_dmesh(*mesh);
+    const int64_t count = int64_t(dm.ext[0]) * dm.ext[1] * dm.ext[2] * array->dofs;
+    int dev = 0, sms = 0;
+    CGX_CUDA(cudaGetDevice(&dev));
+    CGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CGX_CUDA(launch_fill(array->data, array->dtype, count, value, sms, reinterpret_cast<cudaStream_t>(stream)));
+    return CGX_OK;
+}
+
+cgx_status cgx_cartesian_num_bins(const double grid_min[3], const double grid_max[3], const double grid_delta[3],
+                                  int32_t nbin_out[3]) {
+    if (!grid_min || !grid_max || !grid_delta || !nbin_out) return fail(CGX_ERR_INVALID_ARG, "NULL argument");
+    for (int d = 0; d < 3; ++d) {
+        if (!(grid_delta[d] > 0.0) || !(grid_max[d] > grid_min[d]))
+            return fail(CGX_ERR_INVALID_ARG, "grid bounds / delta invalid");
+        // cellsBetween(max, min, 1 / delta) = floor((max - min) * (1 / delta))
+        nbin_out[d] = int32_t(std::floor((grid_max[d] - grid_min[d]) * (1.0 / grid_delta[d])));
+        if (nbin_out[d] < 1) return fail(CGX_ERR_INVALID_ARG, "grid has no cells");
+    }
+    return CGX_OK;
+}
+
+cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions, int64_t begin, int64_t end,
+                                 const double grid_min[3], const double grid_max[3], const double grid_delta[3],
+                                 int32_t* counts, uint64_t* offsets, uint64_t* permutes, void* stream) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    cgx_status s = check_field(positions, "positions");
+    if (s) return s;
+    if (positions->dtype != CGX_F64) return fail(CGX_ERR_INVALID_ARG, "positions must be double");
+    if (begin < 0 || end < begin) return fail(CGX_ERR_INVALID_ARG, "need 0 <= begin <= end");
+    if (end - begin >= (int64_t(1) << 32)) return fail(CGX_ERR_NOT_SUPPORTED, "more than 2^32 - 1 particles");
+    if (!counts || !offsets || (!permutes && end > begin)) return fail(CGX_ERR_INVALID_ARG, "NULL output");
+    int32_t nx[3];
+    s = cgx_cartesian_num_bins(grid_min, grid_max, grid_delta, nx);
+    if (s) return s;
+    const int64_t ncell = int64_t(nx[0]) * nx[1] * nx[2];
+    if (ncell >= (int64_t(1) << 31)) return fail(CGX_ERR_NOT_SUPPORTED, "more than 2^31 bins");
+    double mn[3], rdx[3];
+    for (int d = 0; d < 3; ++d) {
+        mn[d] = grid_min[d];
+        const double dx = (grid_max[d] - grid_min[d]) / nx[d];
+        rdx[d] = 1.0 / dx;
+    }
+    const int64_t n = end - begin;
+    const size_t need = size_t(n) * 4 + 256 + radix_sort_scratch_bytes(n) + scan_scratch_bytes(ncell) + 1024;
+    s = ensure_ws(h, need);
+    if (s) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    char* p = reinterpret_cast<char*>(h->ws);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(p);
+    p = align256(p + size_t(n) * 4);
+    void* scratch = p;
+    CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
+    CGX_CUDA(cudaMemsetAsync(counts, 0, size_t(ncell) * sizeof(int32_t), st));
+    CGX_CUDA(cartesian_keys(to_dfield(*positions), begin, end, mn, rdx, nx, keys, counts, h->flags, st, h->sms));
+    CGX_CUDA(exclusive_scan_counts(counts, ncell, offsets, nullptr, scratch, h->sms, st));
+    if (n > 0)
+        CGX_CUDA(radix_sort_pairs(keys, n, key_bits_for(ncell), permutes, nullptr, uint64_t(begin), scratch,
+                                  radix_sort_scratch_bytes(n), h->sms, st));
+    return CGX_OK;
+}
+
+cgx_status cgx_bin_by_key(cgx_handle h, const int32_t* keys, int64_t begin, int64_t end, int32_t nbin,
+                          int32_t* counts, uint64_t* offsets, uint64_t* permutes, void* stream) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    if (begin < 0 || end < begin) return fail(CGX_ERR_INVALID_ARG, "need 0 <= begin <= end");
+    if (nbin < 1) return fail(CGX_ERR_INVALID_ARG, "nbin must be >= 1");
+    if ((!keys || !permutes) && end > begin) return fail(CGX_ERR_INVALID_ARG, "NULL keys / permutes");
+    if (!counts || !offsets) return fail(CGX_ERR_INVALID_ARG, "NULL output");
+    if (end - begin >= (int64_t(1) << 32)) return fail(CGX_ERR_NOT_SUPPORTED, "more than 2^32 - 1 keys");
+    const int64_t n = end - begin;
+    const size_t need = size_t(n) * 4 + 256 + radix_sort_scratch_bytes(n) + scan_scratch_bytes(nbin) + 1024;
+    cgx_status s = ensure_ws(h, need);
+    if (s) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    char* p = reinterpret_cast<char*>(h->ws);
+    uint32_t* k32 = reinterpret_cast<uint32_t*>(p);
+    p = align256(p + size_t(n) * 4);
+    void* scratch = p;
+    CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
+    CGX_CUDA(cudaMemsetAsync(counts, 0, size_t(nbin) * sizeof(int32_t), st));
+    CGX_CUDA(key_histogram(keys, begin, end, k32, counts, nbin, h->flags, st, h->sms));
+    CGX_CUDA(exclusive_scan_counts(counts, nbin, offsets, nullptr, scratch, h->sms, st));
+    if (n > 0)
+        CGX_CUDA(radix_sort_pairs(k32, n, key_bits_for(nbin), permutes, nullptr, uint64_t(begin), scratch,
+                                  radix_sort_scratch_bytes(n), h->sms, st));
+    return finish_check(h, CGX_FLAG_CHECK_BOUNDS, st);
+}
+
+cgx_status cgx_permute(cgx_handle h, const uint64_t* permutes, int64_t begin, int64_t end, const cgx_field* fields,
+                       const int32_t* ncomps, int n_fields, void* stream) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    if (begin < 0 || end < begin) return fail(CGX_ERR_INVALID_ARG, "need 0 <= begin <= end");
+    if (end == begin) return CGX_OK;
+    if (!permutes || !fields || !ncomps || n_fields < 1) return fail(CGX_ERR_INVALID_ARG, "NULL argument");
+    size_t need = 0;
+    for (int f = 0; f < n_fields; ++f) {
+        cgx_status s = check_field(&fields[f], "field");
+        if (s) return s;
+        if (ncomps[f] < 1) return fail(CGX_ERR_INVALID_ARG, "ncomps must be >= 1");
+        const size_t b = size_t(end - begin) * ncomps[f] * (fields[f].dtype == CGX_F64 ? 8 : 4);
+        if (b > need) need = b;
+    }
+    cgx_status s = ensure_ws(h, need);
+    if (s) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    for (int f = 0; f < n_fields; ++f)
+        CGX_CUDA(permute_field(permutes, begin, end, to_dfield(fields[f]), ncomps[f], h->ws, st, h->sms));
+    return CGX_OK;
+}
+
+cgx_status cgx_tiling_init(const cgx_mesh* mesh, int spline_order, const int32_t tile[3], cgx_tiling* out) {
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    if (!tile || !out) return fail(CGX_ERR_INVALID_ARG, "NULL argument");
+    if (spline_order < 0 || spline_order > 6) return fail(CGX_ERR_NOT_SUPPORTED, "spline order must be in [0, 6]");
+    const DMesh dm = to_dmesh(*mesh);
+    int64_t total = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (tile[d] < 1 || tile[d] > 64) return fail(CGX_ERR_INVALID_ARG, "tile extent must be in [1, 64]");
+        out->tile[d] = tile[d];
+        // base nodes range over [0, ext - num_knot]
+        const int nbase = dm.ext[d] - spline_order;
+        out->num_tiles[d] = nbase < 1 ? 1 : (nbase + tile[d] - 1) / tile[d];
+        total *= out->num_tiles[d];
+    }
+    if (total * tile[0] * tile[1] * tile[2] >= (int64_t(1) << 32))
+        return fail(CGX_ERR_NOT_SUPPORTED, "tiling has more than 2^32 base nodes");
+    out->spline_order = spline_order;
+    out->reserved = 0;
+    out->tile_offsets = nullptr;
+    return CGX_OK;
+}
+
+int64_t cgx_tiling_num_offsets(const cgx_tiling* t) {
+    if (!t) return 0;
+    return int64_t(t->num_tiles[0]) * t->num_tiles[1] * t->num_tiles[2] + 1;
+}
+
+cgx_status cgx_sort_tiles(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point,
+                          cgx_tiling* tiling, uint64_t* permutes, void* stream) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    s = check_field(points, "points");
+    if (s) return s;
+    if (points->dtype != CGX_F64) return fail(CGX_ERR_INVALID_ARG, "point coordinates must be double");
+    if (!tiling || !tiling->tile_offsets) return fail(CGX_ERR_INVALID_ARG, "tiling / tile_offsets is NULL");
+    if (num_point < 0 || num_point >= (int64_t(1) << 32)) return fail(CGX_ERR_NOT_SUPPORTED, "num_point out of range");
+    if (num_point > 0 && !permutes) return fail(CGX_ERR_INVALID_ARG, "permutes is NULL");
+    const int64_t nt = cgx_tiling_num_offsets(tiling) - 1;
+    const int64_t cpt = int64_t(tiling->tile[0]) * tiling->tile[1] * tiling->tile[2];
+    const size_t need = size_t(num_point) * 4 + 256 + size_t(nt) * 4 + 256 + radix_sort_scratch_bytes(num_point) +
+                        size_t(nt) * 8 + scan_scratch_bytes(nt) + 4096;
+    s = ensure_ws(h, need);
+    if (s) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    char* p = reinterpret_cast<char*>(h->ws);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(p);
+    p = align256(p + size_t(num_point) * 4);
+    int32_t* tcounts = reinterpret_cast<int32_t*>(p);
+    p = align256(p + size_t(nt) * 4);
+    void* scratch = p;
+    const DMesh dm = to_dmesh(*mesh);
+    CGX_CUDA(cudaMemsetAsync(tcounts, 0, size_t(nt) * 4, st));
+    CGX_CUDA(tile_keys(dm, to_dfield(*points), num_point, tiling->spline_order, tiling->tile, tiling->num_tiles, keys,
+                       tcounts, st, h->sms));
+    CGX_CUDA(counts_to_int64_offsets(tcounts, nt, tiling->tile_offsets, scratch, st, h->sms));
+    if (num_point > 0)
+        CGX_CUDA(radix_sort_pairs(keys, num_point, key_bits_for(nt * cpt), permutes, nullptr, 0, scratch,
+                                  radix_sort_scratch_bytes(num_point), h->sms, st));
+    return CGX_OK;
+}
+
+}  // extern "C"

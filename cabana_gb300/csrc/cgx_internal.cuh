@@ -1,0 +1,219 @@
+// Internal device-side types and helpers shared by the cgx kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/cgx.h"
+
+namespace cgx {
+
+constexpr int kMaxOps = 8;
+constexpr int kMaxKnot = 7;
+
+// ---------------------------------------------------------------------------
+// Point fields and grid arrays in device-friendly form.
+// ---------------------------------------------------------------------------
+struct DField {
+    char* data;
+    int32_t dtype;
+    int32_t log2vl;  // log2(vector_length)
+    int64_t soa_stride;
+    int64_t comp_stride;
+};
+
+struct DArray {
+    char* data;
+    int32_t dtype;
+    int32_t dofs;
+};
+
+struct DOp {
+    int32_t kind;
+    int32_t slot;  // index of the distinct target array (tiled kernels)
+    double mult;
+    DField x;
+    DArray a;
+};
+
+// Geometry the kernels need, precomputed on the host exactly as
+// evaluateSpline does (grid/src/Cabana_Grid_Splines.hpp:1293-1311):
+// low = coordinates(Entity, {0,0,0}), dx = coordinates({1,1,1}) - low,
+// rdx = 1 / dx.
+struct DMesh {
+    double low[3];
+    double rdx[3];
+    float rdx_f[3];
+    int32_t ext[3];  // ghosted entity extents
+};
+
+__host__ __device__ inline int first_offset(int order) {
+    return (order % 2 == 0) ? -(order / 2) : -((order - 1) / 2);
+}
+
+__device__ __forceinline__ int64_t field_offset(const DField& f, int64_t p, int c) {
+    const int64_t s = p >> f.log2vl;
+    const int64_t a = p & ((int64_t(1) << f.log2vl) - 1);
+    return s * f.soa_stride + a + int64_t(c) * f.comp_stride;
+}
+
+template <class T>
+__device__ __forceinline__ T load_field(const DField& f, int64_t p, int c) {
+    const int64_t o = field_offset(f, p, c);
+    if (f.dtype == CGX_F64) return T(__ldg(reinterpret_cast<const double*>(f.data) + o));
+    return T(__ldg(reinterpret_cast<const float*>(f.data) + o));
+}
+
+template <class T>
+__device__ __forceinline__ void add_field(const DField& f, int64_t p, int c, T v) {
+    const int64_t o = field_offset(f, p, c);
+    if (f.dtype == CGX_F64) {
+        double* ptr = reinterpret_cast<double*>(f.data) + o;
+        *ptr += double(v);
+    } else {
+        float* ptr = reinterpret_cast<float*>(f.data) + o;
+        *ptr += float(v);
+    }
+}
+
+__device__ __forceinline__ int64_t node_index(const DMesh& m, int i, int j, int k) {
+    return (int64_t(i) * m.ext[1] + j) * m.ext[2] + k;
+}
+
+template <class T>
+__device__ __forceinline__ void atomic_add_array(const DArray& a, int64_t node, int dof, T v) {
+    const int64_t o = node * a.dofs + dof;
+    if (a.dtype == CGX_F64)
+        atomicAdd(reinterpret_cast<double*>(a.data) + o, double(v));
+    else
+        atomicAdd(reinterpret_cast<float*>(a.data) + o, float(v));
+}
+
+template <class T>
+__device__ __forceinline__ T load_array(const DArray& a, int64_t node, int dof) {
+    const int64_t o = node * a.dofs + dof;
+    if (a.dtype == CGX_F64) return T(reinterpret_cast<const double*>(a.data)[o]);
+    return T(reinterpret_cast<const float*>(a.data)[o]);
+}
+
+// ---------------------------------------------------------------------------
+// Spline<N> weights.
+//
+// Double form: the reference arithmetic of Splines.hpp:122-452 applied to
+// the logical coordinate x0 (orders 0-3), Cox-de Boor for orders 4-6.
+// Float form: the same polynomials evaluated in FP32 on the in-cell offset
+// u = x0 - int(x0), formed beforehand from the double coordinate.
+// ---------------------------------------------------------------------------
+
+// b[j] = B_d(u + d - j): the d+1 uniform B-spline basis values on one cell.
+template <int D, class T>
+__device__ __forceinline__ void de_boor(T u, T* b) {
+    b[0] = T(1);
+#pragma unroll
+    for (int d = 1; d <= D; ++d) {
+        T nb[D + 1];
+#pragma unroll
+        for (int j = 0; j <= d; ++j) {
+            T left = (j >= 1) ? (u + T(d - j)) * b[j - 1] : T(0);
+            T right = (j <= d - 1) ? (T(1 + j) - u) * b[j] : T(0);
+            nb[j] = (left + right) * (T(1) / T(d));
+        }
+#pragma unroll
+        for (int j = 0; j <= d; ++j) b[j] = nb[j];
+    }
+}
+
+template <int ORDER, class T>
+struct SplineKernel {
+    static constexpr int nk = ORDER + 1;
+
+    // u: in-cell offset in [0, 1); r: 1/dx.
+    __device__ __forceinline__ static void weights(T u, T r, T* w, T* g) {
+        if constexpr (ORDER == 0) {
+            w[0] = T(1);
+            g[0] = T(0);
+        } else if constexpr (ORDER == 1) {
+            w[0] = T(1) - u;
+            w[1] = u;
+            g[0] = -r;
+            g[1] = r;
+        } else if constexpr (ORDER == 2) {
+            const T nine_eights = T(9.0 / 8.0);
+            T xn = u + T(0.5);
+            w[0] = T(0.5) * xn * xn - T(1.5) * xn + nine_eights;
+            g[0] = (xn - T(1.5)) * r;
+            xn -= T(1);
+            w[1] = -xn * xn + T(0.75);
+            g[1] = (T(-2) * xn) * r;
+            xn -= T(1);
+            w[2] = T(0.5) * xn * xn + T(1.5) * xn + nine_eights;
+            g[2] = (xn + T(1.5)) * r;
+        } else if constexpr (ORDER == 3) {
+            const T one_sixth = T(1.0 / 6.0);
+            const T two_thirds = one_sixth * T(4);
+            const T four_thirds = two_thirds * T(2);
+            T xn = u + T(1);
+            T xn2 = xn * xn;
+            w[0] = -xn * xn2 * one_sixth + xn2 - T(2) * xn + four_thirds;
+            g[0] = (T(-0.5) * xn * xn + T(2) * xn - T(2)) * r;
+            xn -= T(1);
+            xn2 = xn * xn;
+            w[1] = T(0.5) * xn * xn2 - xn2 + two_thirds;
+            g[1] = (T(1.5) * xn * xn - T(2) * xn) * r;
+            xn -= T(1);
+            xn2 = xn * xn;
+            w[2] = T(-0.5) * xn * xn2 - xn2 + two_thirds;
+            g[2] = (T(-1.5) * xn * xn - T(2) * xn) * r;
+            xn -= T(1);
+            xn2 = xn * xn;
+            w[3] = xn * xn2 * one_sixth + xn2 + T(2) * xn + four_thirds;
+            g[3] = (T(0.5) * xn * xn + T(2) * xn + T(2)) * r;
+        } else {
+            de_boor<ORDER, T>(u, w);
+            T b[ORDER];
+            de_boor<ORDER - 1, T>(u, b);
+#pragma unroll
+            for (int a = 0; a <= ORDER; ++a) {
+                T left = (a >= 1) ? b[a - 1] : T(0);
+                T right = (a <= ORDER - 1) ? b[a] : T(0);
+                g[a] = (left - right) * r;
+            }
+        }
+    }
+};
+
+// Reference mapping in double: x0 = (xp - low) * rdx (+ 0.5 on the dual grid
+// of even orders), rounded step by step with no contraction so the stencil
+// index is bit-identical to the reference's.
+template <int ORDER>
+__device__ __forceinline__ double logical_coord(double xp, double low, double rdx) {
+    double t = __dmul_rn(__dsub_rn(xp, low), rdx);
+    if constexpr (ORDER % 2 == 0) t = __dadd_rn(t, 0.5);
+    return t;
+}
+
+// Stencil base (first node index) and in-cell offset from the double
+// logical coordinate, as Spline<N>::stencil / value do: int truncation.
+template <int ORDER, class T>
+__device__ __forceinline__ void base_and_offset(double x0, int& base, T& u) {
+    const int c = static_cast<int>(x0);
+    base = c + first_offset(ORDER);
+    u = T(x0 - double(c));
+}
+
+// ---------------------------------------------------------------------------
+// Error flag in device memory (one int per handle). Kernels never trap: a
+// point whose stencil leaves the ghosted index space is skipped and the flag
+// is raised.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void raise_error(int* flag, int code) {
+    if (flag) atomicOr(flag, 1 << code);
+}
+
+inline int log2_int(int v) {
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+}
+
+}  // namespace cgx

@@ -1,0 +1,96 @@
+// Kernel parameter blocks and launcher entry points (host <-> .cu files).
+#pragma once
+
+#include "cgx_internal.cuh"
+
+namespace cgx {
+
+struct PointParams {
+    DMesh mesh;
+    DField points;
+    int64_t num_point;
+    int32_t n_ops;
+    int32_t reserved;
+    int* error_flag;
+    DOp ops[kMaxOps];
+};
+
+struct HaloParams {
+    char* data;
+    int32_t dtype;
+    int32_t dofs;
+    int32_t ext[3];
+    int32_t owned_cells[3];
+    int32_t periodic[3];
+    int32_t halo_width;
+    int32_t node_extra;  // 1 for nodes, 0 for cells
+};
+
+// One distinct grid array touched by a tiled launch.
+struct TiledArray {
+    DArray a;
+    int32_t smem_offset;  // float offset of this array's node box in shared memory
+    int32_t reserved;
+};
+
+// A unit of tiled work: particles [begin, end) of the tile-major order, all
+// filed under tile `tile`.
+struct WorkItem {
+    int64_t begin;
+    int64_t end;
+    int32_t tile;
+    int32_t reserved;
+};
+
+struct TiledParams {
+    DMesh mesh;
+    DField points;
+    int64_t num_point;
+    int32_t n_ops;
+    int32_t n_arrays;
+    int32_t tile[3];
+    int32_t num_tiles[3];
+    int32_t box[3];        // node box per tile: tile + num_knot - 1
+    int32_t box_nodes;     // box[0] * box[1] * box[2]
+    int32_t smem_floats;   // floats of shared memory used for node boxes
+    int32_t reserved;
+    const WorkItem* work;
+    const int64_t* work_count;  // device: number of work items
+    int* work_counter;          // device: dynamic scheduler counter (zeroed per launch)
+    int* error_flag;
+    DOp ops[kMaxOps];
+    TiledArray arrays[kMaxOps];
+};
+
+cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64, int sms, cudaStream_t st);
+cudaError_t launch_halo(const HaloParams& h, bool scatter, int sms, cudaStream_t st);
+cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st);
+
+cudaError_t launch_tiled(const TiledParams& prm, int order, bool p2g, int sms, size_t smem_bytes, cudaStream_t st);
+
+// Sorting / binning (cgx_sort.cu). Scratch comes from the caller.
+size_t radix_sort_scratch_bytes(int64_t n);
+// Stable sort of (keys, index) by key. keys_in is consumed (may be
+// overwritten). The sorted original indices land in perm_out (uint64).
+cudaError_t radix_sort_pairs(uint32_t* keys_in, int64_t n, int key_bits, uint64_t* perm_out, const uint64_t* vals_in,
+                             uint64_t val_offset, void* scratch, size_t scratch_bytes, int sms, cudaStream_t st);
+size_t scan_scratch_bytes(int64_t n);
+// Exclusive scan of int32 counts into uint64 offsets; also writes the total
+// into offsets_total (device, may be null).
+cudaError_t exclusive_scan_counts(const int32_t* counts, int64_t n, uint64_t* offsets, uint64_t* total, void* scratch,
+                                  int sms, cudaStream_t st);
+cudaError_t cartesian_keys(const DField& pos, int64_t begin, int64_t end, const double* mn, const double* rdx,
+                           const int32_t* nx, uint32_t* keys, int32_t* counts, int* error_flag, cudaStream_t st,
+                           int sms);
+cudaError_t key_histogram(const int32_t* keys, int64_t begin, int64_t end, uint32_t* keys_out, int32_t* counts,
+                          int32_t nbin, int* error_flag, cudaStream_t st, int sms);
+cudaError_t permute_field(const uint64_t* perm, int64_t begin, int64_t end, const DField& f, int ncomp, void* scratch,
+                          cudaStream_t st, int sms);
+cudaError_t tile_keys(const DMesh& mesh, const DField& pts, int64_t n, int order, const int32_t* tile,
+                      const int32_t* num_tiles, uint32_t* keys, int32_t* tile_counts, cudaStream_t st, int sms);
+cudaError_t build_work_items(const int64_t* tile_offsets, int64_t num_tiles, int64_t chunk, int64_t* work_prefix,
+                             WorkItem* work, int64_t* work_count, void* scan_scratch, cudaStream_t st, int sms);
+cudaError_t counts_to_int64_offsets(const int32_t* counts, int64_t n, int64_t* offsets, void* scratch, cudaStream_t st,
+                                    int sms);
+
+}  // namespace cgx

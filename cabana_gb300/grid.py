@@ -1,0 +1,329 @@
+"""Cabana::Grid interpolation API over torch CUDA tensors.
+
+Mirrors the reference's call shapes (grid/src/Cabana_Grid_Interpolation.hpp):
+
+    p2g(functor, points, num_point, Spline(N), halo, array)
+    g2p(array, halo, points, num_point, Spline(N), functor)
+
+with the ten functor factories (createScalarValueP2G, ..., createVector
+DivergenceG2P), Array / ArrayLayout / createArray, createHalo and
+ArrayOp.assign. Every call goes through libcgx.so's C ABI; there is no
+Python or PyTorch compute path. Beyond the reference signature, p2g / g2p
+accept a list of functors (one launch, one spline evaluation) and the
+keyword arguments `precision` and `tiling`.
+
+Particle fields are torch tensors indexed (p), (p, d) or (p, m, n) in any
+row-major layout, or `Slice` objects describing AoSoA members.
+"""
+import ctypes
+from dataclasses import dataclass
+from typing import Optional
+
+import torch
+
+from . import _lib as L
+from . import mesh as M
+from .mesh import (Cell, Node, createGlobalGrid, createLocalGrid, createLocalMesh,  # noqa: F401  (re-exported API)
+                   createUniformGlobalMesh)
+
+PLAIN_FP64 = L.CGX_PLAIN_FP64
+FP32_COMPENSATED = L.CGX_FP32_COMPENSATED
+
+
+class Own:
+    """Decomposition tag (Cabana::Grid::Own)."""
+
+
+class Ghost:
+    """Decomposition tag (Cabana::Grid::Ghost)."""
+
+
+@dataclass(frozen=True)
+class Spline:
+    """Cabana::Grid::Spline<order> tag."""
+    order: int
+
+
+class NodeHaloPattern:
+    """NodeHaloPattern<3>: the 26 face/edge/corner neighbours."""
+
+
+def _dtype_code(t):
+    if t == torch.float64:
+        return L.CGX_F64
+    if t == torch.float32:
+        return L.CGX_F32
+    raise TypeError(f"unsupported dtype {t}; use float32 or float64")
+
+
+@dataclass
+class Slice:
+    """A Cabana::Slice of an AoSoA member: `storage` is the flat tensor of the
+    whole AoSoA (any dtype view of it), `offset` the element offset of member
+    element (0, 0) inside it, `vector_length` the SoA width, `soa_stride` the
+    number of member-type elements per SoA, `comps` the member's flattened
+    extra extent (core/src/Cabana_Slice.hpp:96-190)."""
+    storage: torch.Tensor
+    offset: int
+    vector_length: int
+    soa_stride: int
+    comps: int
+    size: int
+
+    def descriptor(self):
+        f = L.CgxField()
+        f.data = self.storage.data_ptr() + self.offset * self.storage.element_size()
+        f.dtype = _dtype_code(self.storage.dtype)
+        f.vector_length = self.vector_length
+        f.soa_stride = self.soa_stride
+        f.comp_stride = self.vector_length
+        return f
+
+
+def field_descriptor(x):
+    """cgx_field for a tensor (p, ...) or a Slice."""
+    if isinstance(x, Slice):
+        return x.descriptor()
+    if not isinstance(x, torch.Tensor):
+        raise TypeError("particle fields must be torch tensors or Slice objects")
+    if not x.is_cuda:
+        raise ValueError("particle fields must live on the GPU")
+    f = L.CgxField()
+    f.data = x.data_ptr()
+    f.dtype = _dtype_code(x.dtype)
+    f.vector_length = 1
+    f.soa_stride = x.stride(0)
+    if x.dim() == 1:
+        f.comp_stride = 1
+    elif x.dim() == 2:
+        f.comp_stride = x.stride(1)  # LayoutRight (p, d): 1; LayoutLeft: n
+    else:
+        # (p, m, n): the flattened component c = m * N + n must be one stride
+        if x.stride(1) != x.shape[2] * x.stride(2):
+            raise ValueError("a (p, m, n) field needs stride(1) == extent(2) * stride(2)")
+        f.comp_stride = x.stride(2)
+    return f
+
+
+@dataclass
+class ArrayLayout:
+    local_grid: M.LocalGrid
+    dofs: int
+    entity: int
+
+    def mesh_params(self):
+        return M.mesh_params(self.local_grid, self.entity)
+
+
+def createArrayLayout(local_grid, dofs_per_entity, entity=Node):
+    ent = entity.value if hasattr(entity, "value") else int(entity)
+    return ArrayLayout(local_grid, int(dofs_per_entity), ent)
+
+
+class Array:
+    """Cabana::Grid::Array: a (i, j, k, dof) tensor over the ghosted index
+    space (grid/src/Cabana_Grid_Array.hpp:44-300)."""
+
+    def __init__(self, label, layout: ArrayLayout, dtype=torch.float64, device="cuda"):
+        self.label = label
+        self._layout = layout
+        ext = layout.mesh_params().extents()
+        self._view = torch.zeros(ext + (layout.dofs,), dtype=dtype, device=device)
+
+    def layout(self):
+        return self._layout
+
+    def view(self):
+        return self._view
+
+    def descriptor(self):
+        a = L.CgxArray()
+        a.data = self._view.data_ptr()
+        a.dtype = _dtype_code(self._view.dtype)
+        a.dofs = self._layout.dofs
+        return a
+
+    def mesh(self):
+        return L.make_mesh(self._layout.mesh_params())
+
+
+def createArray(label, layout, dtype=torch.float64):
+    return Array(label, layout, dtype)
+
+
+class Halo:
+    """Grid halo for NodeHaloPattern<3> on one rank."""
+
+    def __init__(self, width):
+        self.width = width
+
+    def gather(self, array: Array, stream=None):
+        L.check(L.lib().cgx_halo_gather(ctypes.byref(array.mesh()), ctypes.byref(array.descriptor()),
+                                        _stream(stream)))
+
+    def scatter(self, array: Array, stream=None):
+        L.check(L.lib().cgx_halo_scatter_sum(ctypes.byref(array.mesh()), ctypes.byref(array.descriptor()),
+                                             _stream(stream)))
+
+
+def createHalo(pattern, width, array=None):
+    return Halo(width)
+
+
+class ArrayOp:
+    @staticmethod
+    def assign(array: Array, value, decomposition=Ghost, stream=None):
+        """ArrayOp::assign (grid/src/Cabana_Grid_Array.hpp:431-447)."""
+        if decomposition is Ghost:
+            L.check(L.lib().cgx_array_assign(ctypes.byref(array.mesh()), ctypes.byref(array.descriptor()),
+                                             float(value), _stream(stream)))
+        else:
+            (i0, i1), (j0, j1), (k0, k1) = array.layout().local_grid.ownedSpace(array.layout().entity)
+            array.view()[i0:i1, j0:j1, k0:k1] = value
+
+
+# ---- functors ----------------------------------------------------------
+
+@dataclass
+class Functor:
+    kind: int
+    x: object
+    multiplier: float
+    p2g: bool
+    rank: int
+
+
+def _mk(kind, x, multiplier, p2g, rank):
+    if isinstance(x, torch.Tensor):
+        got = x.dim()
+        if got != rank:
+            # the reference static_asserts on the View rank (Interpolation.hpp:958, :1008, ...)
+            raise TypeError(f"field must be rank {rank}, got rank {got}")
+    return Functor(kind, x, float(multiplier), p2g, rank)
+
+
+def createScalarValueP2G(x, multiplier):
+    return _mk(0, x, multiplier, True, 1)
+
+
+def createVectorValueP2G(x, multiplier):
+    return _mk(1, x, multiplier, True, 2)
+
+
+def createScalarGradientP2G(x, multiplier):
+    return _mk(2, x, multiplier, True, 1)
+
+
+def createVectorDivergenceP2G(x, multiplier):
+    return _mk(3, x, multiplier, True, 2)
+
+
+def createTensorDivergenceP2G(x, multiplier):
+    return _mk(4, x, multiplier, True, 3)
+
+
+def createScalarValueG2P(x, multiplier):
+    return _mk(0, x, multiplier, False, 1)
+
+
+def createVectorValueG2P(x, multiplier):
+    return _mk(1, x, multiplier, False, 2)
+
+
+def createScalarGradientG2P(x, multiplier):
+    return _mk(2, x, multiplier, False, 2)
+
+
+def createVectorGradientG2P(x, multiplier):
+    return _mk(3, x, multiplier, False, 3)
+
+
+def createVectorDivergenceG2P(x, multiplier):
+    return _mk(4, x, multiplier, False, 1)
+
+
+def _stream(stream):
+    if stream is None:
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, torch.cuda.Stream):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+def _ops(functors, arrays):
+    n = len(functors)
+    ops = (L.CgxOp * n)()
+    for i, (f, a) in enumerate(zip(functors, arrays)):
+        ops[i].kind = f.kind
+        ops[i].multiplier = f.multiplier
+        ops[i].x = field_descriptor(f.x)
+        ops[i].array = a.descriptor()
+    return ops
+
+
+def _as_list(v):
+    return list(v) if isinstance(v, (list, tuple)) else [v]
+
+
+def p2g(functor, points, num_point, spline: Spline, halo: Optional[Halo], array, *, precision=PLAIN_FP64,
+        tiling=None, handle=None, stream=None, flags=0, check_bounds=False):
+    """Cabana::Grid::p2g (grid/src/Cabana_Grid_Interpolation.hpp:1217-1313).
+
+    `functor` / `array` may be lists of equal length: functor i scatters into
+    array i, all in one launch. Contributions are added to the arrays; when
+    `halo` is given the scatter(Sum) runs afterwards.
+    """
+    fs, arrs = _as_list(functor), _as_list(array)
+    if len(arrs) == 1 and len(fs) > 1:
+        arrs = arrs * len(fs)
+    if any(not f.p2g for f in fs):
+        raise TypeError("p2g needs P2G functors")
+    mesh = arrs[0].mesh()
+    ops = _ops(fs, arrs)
+    pts = field_descriptor(points)
+    h = handle or L.default_handle()
+    fl = flags | (0 if halo is not None else L.CGX_FLAG_SKIP_HALO) | (L.CGX_FLAG_CHECK_BOUNDS if check_bounds else 0)
+    til = ctypes.byref(tiling.struct) if tiling is not None else None
+    L.check(L.lib().cgx_p2g(h.ptr, ctypes.byref(mesh), ctypes.byref(pts), int(num_point), spline.order, ops,
+                            len(fs), precision, til, fl, _stream(stream)))
+
+
+def g2p(array, halo: Optional[Halo], points, num_point, spline: Spline, functor, *, precision=PLAIN_FP64,
+        tiling=None, handle=None, stream=None, flags=0, check_bounds=False):
+    """Cabana::Grid::g2p (grid/src/Cabana_Grid_Interpolation.hpp:831-927)."""
+    fs, arrs = _as_list(functor), _as_list(array)
+    if len(arrs) == 1 and len(fs) > 1:
+        arrs = arrs * len(fs)
+    if any(f.p2g for f in fs):
+        raise TypeError("g2p needs G2P functors")
+    mesh = arrs[0].mesh()
+    ops = _ops(fs, arrs)
+    pts = field_descriptor(points)
+    h = handle or L.default_handle()
+    fl = flags | (0 if halo is not None else L.CGX_FLAG_SKIP_HALO) | (L.CGX_FLAG_CHECK_BOUNDS if check_bounds else 0)
+    til = ctypes.byref(tiling.struct) if tiling is not None else None
+    L.check(L.lib().cgx_g2p(h.ptr, ctypes.byref(mesh), ctypes.byref(pts), int(num_point), spline.order, ops,
+                            len(fs), precision, til, fl, _stream(stream)))
+
+
+class Tiling:
+    """Tile-major ordering of particles for the tiled kernels."""
+
+    def __init__(self, mesh_params, order, tile=(8, 8, 8), device="cuda"):
+        self.struct = L.CgxTiling()
+        t = (ctypes.c_int32 * 3)(*tile)
+        L.check(L.lib().cgx_tiling_init(ctypes.byref(L.make_mesh(mesh_params)), order, t, ctypes.byref(self.struct)))
+        n = L.lib().cgx_tiling_num_offsets(ctypes.byref(self.struct))
+        self.offsets = torch.zeros(n, dtype=torch.int64, device=device)
+        self.struct.tile_offsets = self.offsets.data_ptr()
+        self.mesh_params = mesh_params
+        self.order = order
+
+    def sort(self, points, num_point, handle=None, stream=None):
+        """Compute the tile-major gather permutation of `points` (uint64 as int64)."""
+        perm = torch.empty(max(1, num_point), dtype=torch.int64, device=self.offsets.device)
+        h = handle or L.default_handle()
+        L.check(L.lib().cgx_sort_tiles(h.ptr, ctypes.byref(L.make_mesh(self.mesh_params)),
+                                       ctypes.byref(field_descriptor(points)), int(num_point),
+                                       ctypes.byref(self.struct), ctypes.c_void_p(perm.data_ptr()), _stream(stream)))
+        return perm[:num_point]

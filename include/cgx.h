@@ -1,0 +1,258 @@
+/*
+ * cgx -- C ABI of the GB300-native particle<->grid interpolation library.
+ *
+ * The entry points replace the device work of Cabana::Grid's interpolation
+ * path. Each declaration names the reference interface it stands in for
+ * (paths relative to the Cabana source tree).
+ *
+ * Conventions
+ *   - All data pointers are device pointers unless stated otherwise. The
+ *     caller owns every particle and grid buffer; the library never frees
+ *     caller memory. Workspace (sort buffers, work lists) lives in a
+ *     cgx_handle and is allocated on demand, grow-only.
+ *   - Calls are asynchronous and stream-ordered on the `stream` argument
+ *     (a cudaStream_t passed as void*; NULL = legacy default stream).
+ *   - Every function returns a cgx_status; 0 is success. No C++ exception
+ *     crosses this boundary. cgx_last_error() gives a message for the last
+ *     failure on the calling thread.
+ *   - A handle may be used by one host thread at a time.
+ */
+#ifndef CGX_H
+#define CGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int cgx_status;
+#define CGX_OK 0
+#define CGX_ERR_INVALID_ARG 1   /* bad pointer / size / kind (host check)      */
+#define CGX_ERR_CUDA 2          /* a CUDA runtime call failed                   */
+#define CGX_ERR_OUT_OF_BOUNDS 3 /* a stencil left the ghosted index space       */
+#define CGX_ERR_TIMEOUT 4       /* a bounded device wait gave up                */
+#define CGX_ERR_NOT_SUPPORTED 5 /* combination not built (e.g. spline order)   */
+#define CGX_ERR_NO_MEMORY 6     /* workspace allocation failed                  */
+
+/* Element types. */
+#define CGX_F32 0
+#define CGX_F64 1
+
+/* Array entity types (Cabana::Grid::Node / Cell). */
+#define CGX_NODE 0
+#define CGX_CELL 1
+
+/* Arithmetic forms of p2g / g2p.
+ * CGX_PLAIN_FP64: one thread per point, double precision throughout, global
+ *   atomics -- the arithmetic the reference's Kokkos CUDA path performs.
+ * CGX_FP32_COMPENSATED: cell index and in-cell offset formed from the double
+ *   coordinates to ~48-bit accuracy, spline weights and products in FP32,
+ *   two-sum compensated per-tile accumulation, one atomic per node and dof
+ *   at each tile flush. */
+#define CGX_PLAIN_FP64 0
+#define CGX_FP32_COMPENSATED 1
+
+/* P2G operator kinds: the functors of
+ * grid/src/Cabana_Grid_Interpolation.hpp:1324-1566. */
+#define CGX_SCALAR_VALUE_P2G 0       /* ScalarValueP2G      :1324-1362 */
+#define CGX_VECTOR_VALUE_P2G 1       /* VectorValueP2G      :1373-1413 */
+#define CGX_SCALAR_GRADIENT_P2G 2    /* ScalarGradientP2G   :1424-1462 */
+#define CGX_VECTOR_DIVERGENCE_P2G 3  /* VectorDivergenceP2G :1473-1513 */
+#define CGX_TENSOR_DIVERGENCE_P2G 4  /* TensorDivergenceP2G :1524-1566 */
+
+/* G2P operator kinds: the functors of
+ * grid/src/Cabana_Grid_Interpolation.hpp:938-1182. */
+#define CGX_SCALAR_VALUE_G2P 0       /* ScalarValueG2P      :938-977   */
+#define CGX_VECTOR_VALUE_G2P 1       /* VectorValueG2P      :988-1028  */
+#define CGX_SCALAR_GRADIENT_G2P 2    /* ScalarGradientG2P   :1039-1079 */
+#define CGX_VECTOR_GRADIENT_G2P 3    /* VectorGradientG2P   :1090-1132 */
+#define CGX_VECTOR_DIVERGENCE_G2P 4  /* VectorDivergenceG2P :1143-1182 */
+
+/* Flags for cgx_p2g / cgx_g2p. */
+#define CGX_FLAG_SKIP_HALO 1u     /* do not run the halo scatter / gather step   */
+#define CGX_FLAG_CHECK_BOUNDS 2u  /* synchronise and report CGX_ERR_OUT_OF_BOUNDS */
+
+/*
+ * The uniform local mesh of one Array, reduced to scalars.
+ * Stands in for LocalMesh<UniformMesh> (grid/src/Cabana_Grid_LocalMesh.hpp:
+ * 61-120) plus the LocalGrid facts the halo needs
+ * (grid/src/Cabana_Grid_LocalGrid_impl.hpp:49-60, :430-466).
+ * Ghosted extents: owned_cells + 2*halo_width + (entity == CGX_NODE).
+ */
+typedef struct cgx_mesh {
+    double ghost_low[3];     /* LocalMesh::lowCorner(Ghost(), d)            */
+    double cell_size[3];     /* GlobalMesh::cellSize(d)                     */
+    int32_t owned_cells[3];  /* GlobalGrid::ownedNumCell(d)                 */
+    int32_t halo_width;      /* LocalGrid::haloCellWidth()                  */
+    int32_t periodic[3];     /* GlobalGrid::isPeriodic(d), one rank         */
+    int32_t entity;          /* CGX_NODE / CGX_CELL of the arrays          */
+} cgx_mesh;
+
+/*
+ * A per-point field: a Kokkos::View (p, ...) or a Cabana::Slice of an AoSoA.
+ * Element (p, c) -- c the flattened component index, row-major over the
+ * field's extra dimensions -- lives at element offset
+ *     (p / vector_length) * soa_stride + (p % vector_length) + c * comp_stride
+ * from `data`. A LayoutRight View (p, C) is {1, C, 1}; a LayoutLeft View is
+ * {1, 1, n}; an AoSoA slice is {VL, sizeof(SoA)/sizeof(T), VL}
+ * (core/src/Cabana_Slice.hpp:96-190, core/src/impl/Cabana_Index.hpp:61-80).
+ */
+typedef struct cgx_field {
+    void* data;
+    int32_t dtype;          /* CGX_F32 / CGX_F64                              */
+    int32_t vector_length;  /* 1, or the AoSoA vector length (a power of two)  */
+    int64_t soa_stride;
+    int64_t comp_stride;
+} cgx_field;
+
+/* A grid Array: Kokkos::View<T****> (i, j, k, dof), LayoutRight, over the
+ * ghosted entity index space (grid/src/Cabana_Grid_Array.hpp:44-300). */
+typedef struct cgx_array {
+    void* data;
+    int32_t dtype;  /* CGX_F32 / CGX_F64 */
+    int32_t dofs;   /* extent(3)         */
+} cgx_array;
+
+/* One operator functor: kind, multiplier, the point field it reads (P2G) or
+ * accumulates into (G2P), and the grid array it scatters into (P2G) or
+ * gathers from (G2P). */
+typedef struct cgx_op {
+    int32_t kind;
+    int32_t reserved;
+    double multiplier;
+    cgx_field x;
+    cgx_array array;
+} cgx_op;
+
+/*
+ * Tile-major particle ordering, produced by cgx_sort_tiles and consumed by
+ * the tiled kernels. Particles are grouped by the base node of their spline
+ * stencil; tiles of tile[0] x tile[1] x tile[2] base nodes are numbered
+ * i-major. Particles of tile t occupy [tile_offsets[t], tile_offsets[t+1])
+ * of the sorted order. The ordering is a performance hint only: a point that
+ * is not inside the tile it was filed under is still interpolated exactly.
+ */
+typedef struct cgx_tiling {
+    int32_t tile[3];
+    int32_t num_tiles[3];
+    int32_t spline_order;
+    int32_t reserved;
+    int64_t* tile_offsets;  /* device, cgx_tiling_num_offsets() entries */
+} cgx_tiling;
+
+typedef struct cgx_context* cgx_handle;
+
+/* ---- lifetime --------------------------------------------------------- */
+cgx_status cgx_create(cgx_handle* out);
+cgx_status cgx_destroy(cgx_handle h);
+const char* cgx_last_error(void);
+const char* cgx_version(void);
+
+/* ---- interpolation ---------------------------------------------------- */
+
+/*
+ * Point-to-grid. Replaces Cabana::Grid::p2g(functor, points, num_point,
+ * Spline<N>(), halo, array) (grid/src/Cabana_Grid_Interpolation.hpp:
+ * 1217-1313), generalised to several functors sharing one spline evaluation
+ * (the fused form of benchmark/grid/Cabana_Grid_InterpolationPerformance.cpp:
+ * 48-69). Contributions are ADDED to the arrays; the caller zeroes them
+ * (ArrayOp::assign). Afterwards the halo scatter(Sum) runs on each distinct
+ * array unless CGX_FLAG_SKIP_HALO is set (a no-op on non-periodic meshes).
+ * `points` must hold double coordinates. `tiling` may be NULL (one thread
+ * per point, any order); with a tiling built for this mesh and order and
+ * precision CGX_FP32_COMPENSATED the tiled kernel runs.
+ */
+cgx_status cgx_p2g(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points,
+                   int64_t num_point, int spline_order, const cgx_op* ops,
+                   int n_ops, int precision, const cgx_tiling* tiling,
+                   unsigned flags, void* stream);
+
+/*
+ * Grid-to-point. Replaces Cabana::Grid::g2p(array, halo, points, num_point,
+ * Spline<N>(), functor) (grid/src/Cabana_Grid_Interpolation.hpp:831-927),
+ * several functors per launch. The halo gather(Replace) runs first on each
+ * distinct array unless CGX_FLAG_SKIP_HALO is set. Results are ADDED to the
+ * point fields: x += multiplier * result.
+ */
+cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points,
+                   int64_t num_point, int spline_order, const cgx_op* ops,
+                   int n_ops, int precision, const cgx_tiling* tiling,
+                   unsigned flags, void* stream);
+
+/* Halo::scatter(exec, ScatterReduce::Sum(), array) and Halo::gather(exec,
+ * array) for NodeHaloPattern<3> on one rank (grid/src/Cabana_Grid_HaloBase.hpp:
+ * 202-760, grid/src/impl/Cabana_Grid_Halo_Mpi.hpp:60-245): periodic
+ * dimensions fold ghosts into (or fill ghosts from) their owned images;
+ * non-periodic dimensions have no neighbour and are left alone. */
+cgx_status cgx_halo_scatter_sum(const cgx_mesh* mesh, const cgx_array* array,
+                                void* stream);
+cgx_status cgx_halo_gather(const cgx_mesh* mesh, const cgx_array* array,
+                           void* stream);
+
+/* ArrayOp::assign(array, value, Ghost()) (grid/src/Cabana_Grid_Array.hpp:
+ * 431-447) over the whole ghosted array. */
+cgx_status cgx_array_assign(const cgx_mesh* mesh, const cgx_array* array,
+                            double value, void* stream);
+
+/* ---- binning ---------------------------------------------------------- */
+
+/* CartesianGrid::init cell counts (core/src/impl/Cabana_CartesianGrid.hpp:
+ * 61-73). Host only. */
+cgx_status cgx_cartesian_num_bins(const double grid_min[3],
+                                  const double grid_max[3],
+                                  const double grid_delta[3],
+                                  int32_t nbin_out[3]);
+
+/*
+ * LinkedCellList::build over [begin, end) (core/src/Cabana_LinkedCellList.hpp:
+ * 652-745): counts[prod(nbin)], offsets[prod(nbin)] (exclusive scan of counts,
+ * relative to `begin`), permutes[end-begin] (original indices in binned
+ * order). Within a bin, particles keep ascending index order -- the order of
+ * the reference's Serial backend -- so the output is deterministic.
+ */
+cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions,
+                                 int64_t begin, int64_t end,
+                                 const double grid_min[3],
+                                 const double grid_max[3],
+                                 const double grid_delta[3], int32_t* counts,
+                                 uint64_t* offsets, uint64_t* permutes,
+                                 void* stream);
+
+/* binByKey(keys, nbin, begin, end) (core/src/Cabana_Sort.hpp:164-226) with
+ * a stable in-bin order: keys[begin..end) in [0, nbin). */
+cgx_status cgx_bin_by_key(cgx_handle h, const int32_t* keys, int64_t begin,
+                          int64_t end, int32_t nbin, int32_t* counts,
+                          uint64_t* offsets, uint64_t* permutes, void* stream);
+
+/*
+ * permute(BinningData, AoSoA/Slice/View) (core/src/Cabana_Sort.hpp:549-720):
+ * for each field, element i in [begin, end) becomes old element
+ * permutes[i - begin], all components (ncomps[f] of them) moved together.
+ */
+cgx_status cgx_permute(cgx_handle h, const uint64_t* permutes, int64_t begin,
+                       int64_t end, const cgx_field* fields,
+                       const int32_t* ncomps, int n_fields, void* stream);
+
+/* ---- tile ordering for the tiled kernels (no reference counterpart:
+ *      the reference p2g/g2p are order-agnostic) ------------------------ */
+
+/* Fill the host-side fields of a tiling for a mesh / order / tile shape. */
+cgx_status cgx_tiling_init(const cgx_mesh* mesh, int spline_order,
+                           const int32_t tile[3], cgx_tiling* out);
+int64_t cgx_tiling_num_offsets(const cgx_tiling* tiling);
+
+/* Compute tile-major keys of the points, stable-sort them, write the gather
+ * permutation (sorted[i] = original[permutes[i]]) and tiling->tile_offsets.
+ * Apply the permutation to every particle field with cgx_permute. */
+cgx_status cgx_sort_tiles(cgx_handle h, const cgx_mesh* mesh,
+                          const cgx_field* points, int64_t num_point,
+                          cgx_tiling* tiling, uint64_t* permutes,
+                          void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CGX_H */
