@@ -198,7 +198,87 @@ cgx_status halo_all(const cgx_mesh& m, const cgx_op* ops, int n_ops, bool scatte
     return CGX_OK;
 }
 
-constexpr int64_t kChunk = 2048;
+// Lower the P2G functors to accumulation channels (one grid dof each) and
+// group them for the tiled kernel. Value channels receive a * W, gradient
+// channels b . grad W (Interpolation.hpp:437-747):
+//   ScalarValueP2G      -> 1 value channel      a = m f
+//   VectorValueP2G      -> 3 value channels     a = m f_d
+//   ScalarGradientP2G   -> 3 gradient channels  b = m f e_d
+//   VectorDivergenceP2G -> 1 gradient channel   b = m f
+//   TensorDivergenceP2G -> 3 gradient channels  b = m f_{d,:}
+bool plan_channels(TiledParams& prm, const cgx_op* ops, int n_ops, int order) {
+    Channel val[kMaxChannels], grd[kMaxChannels];
+    int nv = 0, ng = 0;
+    auto add = [&](bool gradient, int slot, int dof, int op, const int* comps) {
+        Channel c;
+        c.slot = int8_t(slot);
+        c.dof = int8_t(dof);
+        for (int n = 0; n < 3; ++n) {
+            c.src_op[n] = int8_t(op);
+            c.src_comp[n] = int8_t(comps[n]);
+        }
+        if (gradient)
+            grd[ng++] = c;
+        else
+            val[nv++] = c;
+    };
+    for (int o = 0; o < n_ops; ++o) {
+        const int slot = prm.ops[o].slot;
+        switch (ops[o].kind) {
+            case CGX_SCALAR_VALUE_P2G: {
+                const int c[3] = {0, -1, -1};
+                add(false, slot, 0, o, c);
+                break;
+            }
+            case CGX_VECTOR_VALUE_P2G:
+                for (int d = 0; d < 3; ++d) {
+                    const int c[3] = {d, -1, -1};
+                    add(false, slot, d, o, c);
+                }
+                break;
+            case CGX_SCALAR_GRADIENT_P2G:
+                for (int d = 0; d < 3; ++d) {
+                    const int c[3] = {d == 0 ? 0 : -1, d == 1 ? 0 : -1, d == 2 ? 0 : -1};
+                    add(true, slot, d, o, c);
+                }
+                break;
+            case CGX_VECTOR_DIVERGENCE_P2G: {
+                const int c[3] = {0, 1, 2};
+                add(true, slot, 0, o, c);
+                break;
+            }
+            case CGX_TENSOR_DIVERGENCE_P2G:
+                for (int m = 0; m < 3; ++m) {
+                    const int c[3] = {3 * m, 3 * m + 1, 3 * m + 2};
+                    add(true, slot, m, o, c);
+                }
+                break;
+        }
+    }
+    const int cv = p2g_group_capacity(order, false), cg = p2g_group_capacity(order, true);
+    int n = 0, g = 0;
+    for (int i = 0; i < nv; i += cv) {
+        if (g >= kMaxGroups) return false;
+        prm.groups[g].gradient = 0;
+        prm.groups[g].first = int8_t(n + i);
+        prm.groups[g].count = int8_t(nv - i < cv ? nv - i : cv);
+        ++g;
+    }
+    for (int i = 0; i < nv; ++i) prm.channels[n++] = val[i];
+    for (int i = 0; i < ng; i += cg) {
+        if (g >= kMaxGroups) return false;
+        prm.groups[g].gradient = 1;
+        prm.groups[g].first = int8_t(n + i);
+        prm.groups[g].count = int8_t(ng - i < cg ? ng - i : cg);
+        ++g;
+    }
+    for (int i = 0; i < ng; ++i) prm.channels[n++] = grd[i];
+    prm.n_channels = n;
+    prm.n_groups = g;
+    return true;
+}
+
+constexpr int64_t kChunk = 4096;
 
 cgx_status build_work(cgx_context* h, const cgx_tiling& t, int64_t num_point, cudaStream_t st) {
     const int64_t nt = int64_t(t.num_tiles[0]) * t.num_tiles[1] * t.num_tiles[2];
@@ -288,6 +368,9 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
         }
         prm.n_arrays = n_arrays;
         prm.smem_floats = offset;
+        const int shift_even = (spline_order % 2 == 0) ? 1 : 0;
+        for (int d = 0; d < 3; ++d) prm.c0[d] = -dm.low[d] * dm.rdx[d] + 0.5 * shift_even;
+        if (p2g && !plan_channels(prm, ops, n_ops, spline_order)) tiled = false;  // too many channel groups
         const size_t smem = size_t(offset) * sizeof(float);
         if (smem > 200 * 1024) tiled = false;  // box too large: use the point kernel
         if (tiled) {
@@ -298,7 +381,10 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
             prm.work_counter = h->flags + 1;
             prm.error_flag = h->flags;
             CGX_CUDA(cudaMemsetAsync(h->flags + 1, 0, sizeof(int), st));
-            CGX_CUDA(launch_tiled(prm, spline_order, p2g, h->sms, smem, st));
+            if (p2g)
+                CGX_CUDA(launch_p2g_tiled(prm, spline_order, h->sms, smem, st));
+            else
+                CGX_CUDA(launch_tiled(prm, spline_order, false, h->sms, smem, st));
         }
     }
     if (!tiled && num_point > 0) {

@@ -201,6 +201,40 @@ __device__ __forceinline__ void base_and_offset(double x0, int& base, T& u) {
     u = T(x0 - double(c));
 }
 
+// Integer part and in-cell offset of a non-negative logical coordinate t
+// held in a double, using integer operations only (the double pipe runs at
+// 1/64 of the FP32 rate on this part). The offset is truncated to 32
+// fraction bits, then to FP32 toward zero, so it is always < 1. Returns
+// false for t < 0, t >= 2^30 or NaN.
+__device__ __forceinline__ bool split_logical(double t, int& cell, float& u) {
+    if (!(t >= 0.0) || !(t < 1073741824.0)) {
+        cell = 0;
+        u = 0.0f;
+        return false;
+    }
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(t));
+    const int e = int(b >> 52);
+    if (e == 0) {  // zero or subnormal
+        cell = 0;
+        u = 0.0f;
+        return true;
+    }
+    const unsigned long long sig = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 1075 - e;  // t = sig * 2^-sh
+    unsigned int ufx;
+    if (sh > 52) {  // t < 1
+        cell = 0;
+        const int r = sh - 32;
+        ufx = r >= 53 ? 0u : static_cast<unsigned int>(sig >> r);
+    } else {
+        cell = int(sig >> sh);
+        const unsigned long long fr = sig & ((1ull << sh) - 1ull);
+        ufx = sh >= 32 ? static_cast<unsigned int>(fr >> (sh - 32)) : static_cast<unsigned int>(fr << (32 - sh));
+    }
+    u = __uint2float_rz(ufx) * 2.3283064365386963e-10f;  // * 2^-32
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // Error flag in device memory (one int per handle). Kernels never trap: a
 // point whose stencil leaves the ghosted index space is skipped and the flag

@@ -42,8 +42,30 @@ struct WorkItem {
     int32_t reserved;
 };
 
+// One accumulation channel of a tiled p2g launch: a dof of a target array
+// that receives, per point, either a * W (value channel) or b . grad W
+// (gradient channel). Sources name (op, component); comp < 0 means zero.
+struct Channel {
+    int8_t slot;
+    int8_t dof;
+    int8_t src_op[3];
+    int8_t src_comp[3];
+};
+
+// A set of channels processed together by one warp role.
+struct ChannelGroup {
+    int8_t gradient;  // 0: value channels, 1: gradient channels
+    int8_t first;
+    int8_t count;
+    int8_t reserved;
+};
+
+constexpr int kMaxChannels = 24;
+constexpr int kMaxGroups = 16;
+
 struct TiledParams {
     DMesh mesh;
+    double c0[3];  // -low * rdx + (0.5 for even orders): t = fma(x, rdx, c0)
     DField points;
     int64_t num_point;
     int32_t n_ops;
@@ -60,6 +82,10 @@ struct TiledParams {
     int* error_flag;
     DOp ops[kMaxOps];
     TiledArray arrays[kMaxOps];
+    int32_t n_channels;
+    int32_t n_groups;
+    Channel channels[kMaxChannels];
+    ChannelGroup groups[kMaxGroups];
 };
 
 cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64, int sms, cudaStream_t st);
@@ -67,6 +93,9 @@ cudaError_t launch_halo(const HaloParams& h, bool scatter, int sms, cudaStream_t
 cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st);
 
 cudaError_t launch_tiled(const TiledParams& prm, int order, bool p2g, int sms, size_t smem_bytes, cudaStream_t st);
+cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem_bytes, cudaStream_t st);
+// Channels per group of the tiled p2g kernel for a spline order.
+int p2g_group_capacity(int order, bool gradient);
 
 // Sorting / binning (cgx_sort.cu). Scratch comes from the caller.
 size_t radix_sort_scratch_bytes(int64_t n);

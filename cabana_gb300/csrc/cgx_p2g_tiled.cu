@@ -1,0 +1,403 @@
+// Tiled point-to-grid for particles in tile-major order (FP32-compensated form).
+//
+// The work is the reference's P2G::value / gradient / divergence scatter
+// (grid/src/Cabana_Grid_Interpolation.hpp:437-747) for several functors at
+// once, reorganised for a GPU whose shared-memory atomics serialise when a
+// warp's lanes hit one address -- which is exactly what happens when the
+// particles of a warp share a cell:
+//
+//  * Operators are lowered to channels: one grid dof that receives, per
+//    point, a * W (value channel) or b . grad W (gradient channel). Channels
+//    are grouped (up to 4 value or 3 gradient channels per group for the
+//    quadratic spline) and each warp of the CTA takes one group, so a lane
+//    holds the group's whole stencil (27 nodes x channels) in registers.
+//  * A warp walks its run of sorted particles 32 at a time, one particle per
+//    lane. While all lanes of a window share one stencil base node, each lane
+//    adds its particle into its registers; when the base node changes the
+//    warp reduces the registers across lanes with a transpose-reduction
+//    (each lane ends with 1/32 of the sums) and adds them into the tile's
+//    shared node box with compensated atomics: one shared atomic per node
+//    and channel per run instead of one per particle.
+//  * Windows whose lanes straddle several base nodes add each particle
+//    directly (compensated shared atomics); points outside the tile's box go
+//    straight to global memory with bounds checks, so the tile ordering
+//    never changes the result.
+//  * At the end of a work item the box is flushed to the Array, one atomic
+//    per touched node and dof, sum and compensation rounded once.
+//
+// The cell index and in-cell offset are formed with one double FMA per
+// dimension and integer operations; weights and products are FP32.
+#include "cgx_kernels.cuh"
+
+namespace cgx {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxRunWindows = 16;  // register sums cover at most 16 windows per lane
+
+template <int ORDER>
+struct P2GShape {
+    static constexpr int K = ORDER + 1;
+    static constexpr int NODES = K * K * K;
+    static constexpr int CV = ORDER >= 3 ? 2 : 4;  // value channels per group
+    static constexpr int CG = ORDER >= 3 ? 1 : 3;  // gradient channels per group
+    static constexpr int pad32(int v) { return (v + 31) / 32 * 32; }
+    static constexpr int NV = pad32(NODES * CV);
+    static constexpr int NG = pad32(NODES * CG);
+};
+
+__device__ __forceinline__ void comp_add(float* sum, float* comp, float v) {
+    const float old = atomicAdd(sum, v);
+    const float s = old + v;
+    const float bp = s - old;
+    const float e = (old - (s - bp)) + (v - bp);
+    if (e != 0.0f) atomicAdd(comp, e);
+}
+
+// After the call lane L holds, in v[0 .. N/32), the sums over all lanes of
+// the original v[L*N/32 .. (L+1)*N/32).
+template <int HALF, int O>
+__device__ __forceinline__ void reduce_level(float* v, int lane) {
+    const bool upper = (lane & O) != 0;
+#pragma unroll
+    for (int i = 0; i < HALF; ++i) {
+        const float send = upper ? v[i] : v[i + HALF];
+        const float keep = upper ? v[i + HALF] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void transpose_reduce(float* v, int lane) {
+    reduce_level<N / 2, 16>(v, lane);
+    reduce_level<N / 4, 8>(v, lane);
+    reduce_level<N / 8, 4>(v, lane);
+    reduce_level<N / 16, 2>(v, lane);
+    reduce_level<N / 32, 1>(v, lane);
+}
+
+// Shared-memory offsets of each channel's dof in the node box.
+struct ChanSmem {
+    int sum_base;  // float offset of (node 0, dof) in the sum half
+    int comp_off;  // distance from the sum half to the compensation half
+    int dofs;      // node stride
+};
+
+struct PointState {
+    double x[3];
+    bool valid;
+};
+
+template <int ORDER>
+__device__ __forceinline__ bool form_point(const TiledParams& prm, const double* x, int* s, float* u) {
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        int c;
+        ok &= split_logical(t, c, u[d]);
+        s[d] = c + first_offset(ORDER);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
+    }
+    return ok;
+}
+
+__device__ __forceinline__ float chan_src(const TiledParams& prm, int op, int comp, int64_t p) {
+    if (comp < 0) return 0.0f;
+    const DOp& o = prm.ops[op];
+    return load_field<float>(o.x, p, comp) * float(o.mult);
+}
+
+// Direct (per-point) contribution of one group: compensated shared atomics
+// into the box, or global atomics when the stencil is outside the box.
+template <int ORDER, int CH, bool GRAD>
+__device__ __forceinline__ void add_direct(const TiledParams& prm, float* smem, const ChanSmem* cs, int first,
+                                           int count, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
+                                           const float (*coef)[3], bool inbox, const int* l, const int* s) {
+    constexpr int K = ORDER + 1;
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                float wv = 0.0f, g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
+                if (GRAD) {
+                    g0 = g[0][i] * w[1][j] * w[2][k];
+                    g1 = w[0][i] * g[1][j] * w[2][k];
+                    g2 = w[0][i] * w[1][j] * g[2][k];
+                } else {
+                    wv = w[0][i] * w[1][j] * w[2][k];
+                }
+                const int bnode = inbox ? ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k) : 0;
+                const int64_t gnode = inbox ? 0 : node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+#pragma unroll
+                for (int c = 0; c < CH; ++c) {
+                    if (c >= count) break;
+                    const float v = GRAD ? coef[c][0] * g0 + coef[c][1] * g1 + coef[c][2] * g2 : coef[c][0] * wv;
+                    if (inbox) {
+                        const ChanSmem m = cs[first + c];
+                        const int e = m.sum_base + bnode * m.dofs;
+                        comp_add(smem + e, smem + e + m.comp_off, v);
+                    } else {
+                        const Channel& ch = prm.channels[first + c];
+                        atomic_add_array(prm.arrays[ch.slot].a, gnode, ch.dof, v);
+                    }
+                }
+            }
+}
+
+// Reduce the warp's register sums and add them to the box.
+template <int ORDER, int CH, int NPAD>
+__device__ __forceinline__ void flush_run(float* acc, int lane, int key, const TiledParams& prm, float* smem,
+                                          const ChanSmem* cs, int first, int count) {
+    constexpr int K = ORDER + 1;
+    constexpr int NODES = K * K * K;
+    constexpr int R = NPAD / 32;
+    transpose_reduce<NPAD>(acc, lane);
+    const int l2 = key % prm.box[2];
+    const int l1 = (key / prm.box[2]) % prm.box[1];
+    const int l0 = key / (prm.box[1] * prm.box[2]);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int idx = lane * R + r;
+        const int node = idx / CH;
+        const int c = idx - node * CH;
+        if (node < NODES && c < count && acc[r] != 0.0f) {
+            const int i = node / (K * K), j = (node / K) % K, k = node % K;
+            const int bnode = ((l0 + i) * prm.box[1] + (l1 + j)) * prm.box[2] + (l2 + k);
+            const ChanSmem m = cs[first + c];
+            const int e = m.sum_base + bnode * m.dofs;
+            comp_add(smem + e, smem + e + m.comp_off, acc[r]);
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
+}
+
+// One warp processes particles [b, e) of the current work item for one group.
+template <int ORDER, bool GRAD>
+__device__ __forceinline__ void run_group(const TiledParams& prm, float* smem, const ChanSmem* cs, int gi,
+                                          const int* origin, int64_t b, int64_t e, int lane) {
+    using SH = P2GShape<ORDER>;
+    constexpr int K = SH::K;
+    constexpr int CH = GRAD ? SH::CG : SH::CV;
+    constexpr int NPAD = GRAD ? SH::NG : SH::NV;
+    const ChannelGroup grp = prm.groups[gi];
+    const int first = grp.first, count = grp.count;
+
+    float acc[NPAD];
+#pragma unroll
+    for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
+    int cur_key = -1;
+    int run_windows = 0;
+
+    for (int64_t w0 = b; w0 < e; w0 += 32) {
+        const int64_t p = w0 + lane;
+        const bool active = p < e;
+        int s[3] = {0, 0, 0};
+        float u[3] = {0.0f, 0.0f, 0.0f};
+        bool ok = false;
+        if (active) {
+            double x[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) x[d] = load_field<double>(prm.points, p, d);
+            ok = form_point<ORDER>(prm, x, s, u);
+            if (!ok) raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+        }
+        int l[3];
+        bool inbox = ok;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            l[d] = s[d] - origin[d];
+            inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
+        }
+        const int key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : -1;
+        const int key0 = __shfl_sync(0xffffffffu, key, 0);
+        const bool uniform = __all_sync(0xffffffffu, !active || (ok && key == key0)) && key0 >= 0;
+
+        float w[3][K], g[3][K];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+        float coef[CH][3];
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            const bool use = ok && c < count;
+            const Channel& ch = prm.channels[first + (c < count ? c : 0)];
+#pragma unroll
+            for (int n = 0; n < 3; ++n) {
+                coef[c][n] = 0.0f;
+                if (n == 0 || GRAD) coef[c][n] = use ? chan_src(prm, ch.src_op[n], ch.src_comp[n], p) : 0.0f;
+            }
+        }
+
+        if (uniform) {
+            if (key0 != cur_key || run_windows == kMaxRunWindows) {
+                if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
+                cur_key = key0;
+                run_windows = 0;
+            }
+            ++run_windows;
+            // Register accumulation; inactive lanes carry zero coefficients.
+#pragma unroll
+            for (int i = 0; i < K; ++i)
+#pragma unroll
+                for (int j = 0; j < K; ++j) {
+                    if (GRAD) {
+                        const float wij = w[0][i] * w[1][j];
+                        const float gi0 = g[0][i] * w[1][j];
+                        const float gi1 = w[0][i] * g[1][j];
+                        float P[CH], Q[CH];
+#pragma unroll
+                        for (int c = 0; c < CH; ++c) {
+                            P[c] = coef[c][0] * gi0 + coef[c][1] * gi1;
+                            Q[c] = coef[c][2] * wij;
+                        }
+#pragma unroll
+                        for (int k = 0; k < K; ++k)
+#pragma unroll
+                            for (int c = 0; c < CH; ++c) {
+                                float& a = acc[((i * K + j) * K + k) * CH + c];
+                                a = fmaf(P[c], w[2][k], fmaf(Q[c], g[2][k], a));
+                            }
+                    } else {
+                        const float wij = w[0][i] * w[1][j];
+                        float A[CH];
+#pragma unroll
+                        for (int c = 0; c < CH; ++c) A[c] = coef[c][0] * wij;
+#pragma unroll
+                        for (int k = 0; k < K; ++k)
+#pragma unroll
+                            for (int c = 0; c < CH; ++c) {
+                                float& a = acc[((i * K + j) * K + k) * CH + c];
+                                a = fmaf(A[c], w[2][k], a);
+                            }
+                    }
+                }
+        } else {
+            if (cur_key >= 0) {
+                flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
+                cur_key = -1;
+                run_windows = 0;
+            }
+            if (ok) add_direct<ORDER, CH, GRAD>(prm, smem, cs, first, count, w, g, coef, inbox, l, s);
+        }
+    }
+    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_constant__ TiledParams prm) {
+    extern __shared__ float smem[];
+    __shared__ ChanSmem cs[kMaxChannels];
+    __shared__ int item_idx;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = threadIdx.x; c < prm.n_channels; c += blockDim.x) {
+        const Channel ch = prm.channels[c];
+        const TiledArray& ta = prm.arrays[ch.slot];
+        cs[c].sum_base = ta.smem_offset + ch.dof;
+        cs[c].comp_off = prm.box_nodes * ta.a.dofs;
+        cs[c].dofs = ta.a.dofs;
+    }
+    const int64_t nwork = *prm.work_count;
+    const int ng = prm.n_groups;
+    const int wpg = ng <= kWarps ? kWarps / ng : 1;  // warps per group
+    while (true) {
+        if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
+        for (int i = threadIdx.x; i < prm.smem_floats; i += blockDim.x) smem[i] = 0.0f;
+        __syncthreads();
+        const int64_t widx = item_idx;
+        if (widx >= nwork) break;
+        const WorkItem it = prm.work[widx];
+        int origin[3];
+        {
+            const int t2 = it.tile % prm.num_tiles[2];
+            const int t1 = (it.tile / prm.num_tiles[2]) % prm.num_tiles[1];
+            const int t0 = it.tile / (prm.num_tiles[1] * prm.num_tiles[2]);
+            origin[0] = t0 * prm.tile[0];
+            origin[1] = t1 * prm.tile[1];
+            origin[2] = t2 * prm.tile[2];
+        }
+        if (ng <= kWarps) {
+            const int gi = warp / wpg;
+            if (gi < ng) {
+                const int r = warp % wpg;
+                const int64_t len = it.end - it.begin;
+                const int64_t per = ((len + wpg - 1) / wpg + 31) / 32 * 32;
+                const int64_t b = it.begin + r * per;
+                const int64_t e = (b + per < it.end) ? b + per : it.end;
+                if (b < e) {
+                    if (prm.groups[gi].gradient)
+                        run_group<ORDER, true>(prm, smem, cs, gi, origin, b, e, lane);
+                    else
+                        run_group<ORDER, false>(prm, smem, cs, gi, origin, b, e, lane);
+                }
+            }
+        } else {
+            for (int gi = warp; gi < ng; gi += kWarps) {
+                if (prm.groups[gi].gradient)
+                    run_group<ORDER, true>(prm, smem, cs, gi, origin, it.begin, it.end, lane);
+                else
+                    run_group<ORDER, false>(prm, smem, cs, gi, origin, it.begin, it.end, lane);
+            }
+        }
+        __syncthreads();
+        // Flush the box: one atomic per touched node and dof.
+        for (int slot = 0; slot < prm.n_arrays; ++slot) {
+            const TiledArray& ta = prm.arrays[slot];
+            const int dofs = ta.a.dofs;
+            const int count = prm.box_nodes * dofs;
+            const float* sum = smem + ta.smem_offset;
+            const float* comp = sum + count;
+            for (int e = threadIdx.x; e < count; e += blockDim.x) {
+                const float v = sum[e] + comp[e];
+                if (v == 0.0f) continue;
+                const int node = e / dofs, dof = e - node * dofs;
+                const int bk = node % prm.box[2];
+                const int bj = (node / prm.box[2]) % prm.box[1];
+                const int bi = node / (prm.box[1] * prm.box[2]);
+                const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
+                if (gi >= prm.mesh.ext[0] || gj >= prm.mesh.ext[1] || gk >= prm.mesh.ext[2]) continue;
+                atomic_add_array(ta.a, node_index(prm.mesh, gi, gj, gk), dof, v);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int ORDER>
+cudaError_t launch_order(const TiledParams& prm, int sms, size_t smem, cudaStream_t st) {
+    const void* fn = reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER>);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    p2g_tiled_kernel<ORDER><<<sms * per_sm, kThreads, smem, st>>>(prm);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int p2g_group_capacity(int order, bool gradient) {
+    switch (order) {
+        case 1: return gradient ? P2GShape<1>::CG : P2GShape<1>::CV;
+        case 2: return gradient ? P2GShape<2>::CG : P2GShape<2>::CV;
+        case 3: return gradient ? P2GShape<3>::CG : P2GShape<3>::CV;
+    }
+    return 0;
+}
+
+cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem, cudaStream_t st) {
+    switch (order) {
+        case 1: return launch_order<1>(prm, sms, smem, st);
+        case 2: return launch_order<2>(prm, sms, smem, st);
+        case 3: return launch_order<3>(prm, sms, smem, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace cgx

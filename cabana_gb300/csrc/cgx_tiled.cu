@@ -1,234 +1,170 @@
-// Tiled p2g / g2p for particles in tile-major order (the FP32-compensated
-// form).
+// Tiled grid-to-point for particles in tile-major order (FP32 form).
 //
 // A persistent grid pulls work items (a tile and a contiguous run of its
-// particles) from a device counter. For p2g a CTA accumulates the run into a
-// shared-memory node box (the tile's base nodes plus the stencil reach) with
-// two-sum compensation, then flushes the box to the Array with one atomic per
-// node and dof. For g2p the CTA stages the node box of every source array in
-// shared memory and gathers from it. A point whose stencil leaves the box
-// (one filed under the wrong tile) goes straight to global memory, so the
-// ordering only affects speed, never the result.
-//
-// Same arithmetic as Cabana::Grid::P2G / G2P (grid/src/Cabana_Grid_
-// Interpolation.hpp:53-747) in FP32 with the cell index and in-cell offset
-// formed in double.
+// particles) from a device counter. The CTA stages the tile's node box of
+// every source array in shared memory with coalesced loads, then each thread
+// gathers for one particle at a time. All operators that read one array share
+// a single pass over the stencil that forms, per dof n, the value sum
+// V_n = sum W v_n and the gradient sums D_mn = sum d_m W v_n in factorised
+// (tensor-product) order; each functor then takes its result from them:
+//   ScalarValueG2P V_0, VectorValueG2P V_n, ScalarGradientG2P D_m0,
+//   VectorGradientG2P D_mn, VectorDivergenceG2P sum_m D_mm
+// (grid/src/Cabana_Grid_Interpolation.hpp:53-364, :938-1182).
+// A point whose stencil leaves the box reads the Array directly, so the
+// ordering never changes the result.
 #include "cgx_kernels.cuh"
 
 namespace cgx {
 
 namespace {
 
-// Compensated accumulation into a (sum, comp) pair held in shared memory.
-// atomicAdd returns the value it replaced, so the rounding error of that
-// very addition can be recovered exactly (TwoSum) and kept in `comp`.
-__device__ __forceinline__ void comp_add(float* sum, float* comp, float v) {
-    const float old = atomicAdd(sum, v);
-    const float s = old + v;
-    const float bp = s - old;
-    const float e = (old - (s - bp)) + (v - bp);
-    if (e != 0.0f) atomicAdd(comp, e);
-}
+constexpr int kThreads = 256;
 
-struct Box {
-    int origin[3];  // first base node of the tile
-    int box[3];
-};
-
-__device__ __forceinline__ void tile_origin(const TiledParams& prm, int tile, int* origin) {
-    const int t2 = tile % prm.num_tiles[2];
-    const int t1 = (tile / prm.num_tiles[2]) % prm.num_tiles[1];
-    const int t0 = tile / (prm.num_tiles[1] * prm.num_tiles[2]);
-    origin[0] = t0 * prm.tile[0];
-    origin[1] = t1 * prm.tile[1];
-    origin[2] = t2 * prm.tile[2];
-}
-
-// Form base node and FP32 weights of point p. Returns false (and raises the
-// error flag) when the stencil leaves the ghosted index space.
 template <int ORDER>
-__device__ __forceinline__ bool point_weights(const TiledParams& prm, int64_t p, int* s, float (*w)[ORDER + 1],
-                                              float (*g)[ORDER + 1]) {
-    constexpr int nk = ORDER + 1;
+__device__ __forceinline__ bool form_point(const TiledParams& prm, const double* x, int* s, float* u) {
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double x0 = logical_coord<ORDER>(load_field<double>(prm.points, p, d), prm.mesh.low[d], prm.mesh.rdx[d]);
-        float u;
-        base_and_offset<ORDER, float>(x0, s[d], u);
-        ok &= (x0 >= 0.0) && (s[d] >= 0) && (s[d] + nk <= prm.mesh.ext[d]);
-        SplineKernel<ORDER, float>::weights(u, prm.mesh.rdx_f[d], w[d], g[d]);
+        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        int c;
+        ok &= split_logical(t, c, u[d]);
+        s[d] = c + first_offset(ORDER);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
     }
-    if (!ok) raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
     return ok;
 }
 
-// Adds v to dof `dof` of node (s + (i,j,k)) of array slot `a`: into the
-// shared box when the stencil is inside it, else straight to global memory.
-struct P2GSink {
-    const TiledParams& prm;
-    float* smem;
-    const int* l;  // local base node inside the box
-    const int* s;  // global base node
-    bool inbox;
-
-    __device__ __forceinline__ void add(int slot, int i, int j, int k, int dof, float v) const {
-        const TiledArray& ta = prm.arrays[slot];
-        if (inbox) {
-            const int node = ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k);
-            const int e = node * ta.a.dofs + dof;
-            float* base = smem + ta.smem_offset;
-            comp_add(base + e, base + prm.box_nodes * ta.a.dofs + e, v);
-        } else {
-            atomic_add_array(ta.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), dof, v);
-        }
+// Gather sums for one array: V[n] = sum W v_n, D[m][n] = sum d_m W v_n.
+template <int ORDER, int NDOF, bool GRAD>
+__device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledArray& ta, const float* box, bool inbox,
+                                            const int* l, const int* s, const float (*w)[ORDER + 1],
+                                            const float (*g)[ORDER + 1], float* V, float (*D)[3]) {
+    constexpr int K = ORDER + 1;
+    const int dofs = ta.a.dofs;
+#pragma unroll
+    for (int n = 0; n < NDOF; ++n) {
+        V[n] = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) D[m][n] = 0.0f;
     }
-};
-
-template <int ORDER>
-__global__ void __launch_bounds__(256) p2g_tiled_kernel(const __grid_constant__ TiledParams prm) {
-    constexpr int nk = ORDER + 1;
-    extern __shared__ float smem[];
-    __shared__ int item_idx;
-    const int64_t nwork = *prm.work_count;
-    while (true) {
-        if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
-        __syncthreads();
-        const int64_t widx = item_idx;
-        if (widx >= nwork) break;
-        const WorkItem it = prm.work[widx];
-        int origin[3];
-        tile_origin(prm, it.tile, origin);
-        for (int i = threadIdx.x; i < prm.smem_floats; i += blockDim.x) smem[i] = 0.0f;
-        __syncthreads();
-
-        for (int64_t p = it.begin + threadIdx.x; p < it.end; p += blockDim.x) {
-            int s[3];
-            float w[3][nk], g[3][nk];
-            if (!point_weights<ORDER>(prm, p, s, w, g)) continue;
-            int l[3];
-            bool inbox = true;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                l[d] = s[d] - origin[d];
-                inbox &= (l[d] >= 0) && (l[d] + nk <= prm.box[d]);
+    for (int i = 0; i < K; ++i) {
+        float Tww[NDOF], Tgw[NDOF], Twg[NDOF];
+#pragma unroll
+        for (int n = 0; n < NDOF; ++n) Tww[n] = Tgw[n] = Twg[n] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            float Sw[NDOF], Sg[NDOF];
+#pragma unroll
+            for (int n = 0; n < NDOF; ++n) Sw[n] = Sg[n] = 0.0f;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                float v[NDOF];
+                if (inbox) {
+                    const int node = ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k);
+#pragma unroll
+                    for (int n = 0; n < NDOF; ++n) v[n] = box[node * dofs + n];
+                } else {
+                    const int64_t node = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+#pragma unroll
+                    for (int n = 0; n < NDOF; ++n) v[n] = load_array<float>(ta.a, node, n);
+                }
+#pragma unroll
+                for (int n = 0; n < NDOF; ++n) {
+                    Sw[n] = fmaf(w[2][k], v[n], Sw[n]);
+                    if (GRAD) Sg[n] = fmaf(g[2][k], v[n], Sg[n]);
+                }
             }
-            const P2GSink sink{prm, smem, l, s, inbox};
-            for (int o = 0; o < prm.n_ops; ++o) {
-                const DOp& op = prm.ops[o];
-                const float mult = float(op.mult);
-                switch (op.kind) {
-                    case CGX_SCALAR_VALUE_P2G: {
-                        const float pd = load_field<float>(op.x, p, 0) * mult;
 #pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j) {
-                                const float wij = pd * w[0][i] * w[1][j];
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) sink.add(op.slot, i, j, k, 0, wij * w[2][k]);
-                            }
-                        break;
-                    }
-                    case CGX_VECTOR_VALUE_P2G: {
-                        float pd[3];
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) pd[d] = mult * load_field<float>(op.x, p, d);
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j) {
-                                const float wij = w[0][i] * w[1][j];
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) {
-                                    const float wijk = wij * w[2][k];
-#pragma unroll
-                                    for (int d = 0; d < 3; ++d) sink.add(op.slot, i, j, k, d, pd[d] * wijk);
-                                }
-                            }
-                        break;
-                    }
-                    case CGX_SCALAR_GRADIENT_P2G: {
-                        const float pd = load_field<float>(op.x, p, 0) * mult;
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j)
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) {
-                                    sink.add(op.slot, i, j, k, 0, pd * g[0][i] * w[1][j] * w[2][k]);
-                                    sink.add(op.slot, i, j, k, 1, pd * w[0][i] * g[1][j] * w[2][k]);
-                                    sink.add(op.slot, i, j, k, 2, pd * w[0][i] * w[1][j] * g[2][k]);
-                                }
-                        break;
-                    }
-                    case CGX_VECTOR_DIVERGENCE_P2G: {
-                        float pd[3];
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) pd[d] = mult * load_field<float>(op.x, p, d);
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j)
-#pragma unroll
-                                for (int k = 0; k < nk; ++k)
-                                    sink.add(op.slot, i, j, k, 0,
-                                             pd[0] * g[0][i] * w[1][j] * w[2][k] + pd[1] * w[0][i] * g[1][j] * w[2][k] +
-                                                 pd[2] * w[0][i] * w[1][j] * g[2][k]);
-                        break;
-                    }
-                    case CGX_TENSOR_DIVERGENCE_P2G: {
-                        float pd[3][3];
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-#pragma unroll
-                            for (int b = 0; b < 3; ++b) pd[a][b] = mult * load_field<float>(op.x, p, a * 3 + b);
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j)
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) {
-                                    const float rg0 = g[0][i] * w[1][j] * w[2][k];
-                                    const float rg1 = w[0][i] * g[1][j] * w[2][k];
-                                    const float rg2 = w[0][i] * w[1][j] * g[2][k];
-#pragma unroll
-                                    for (int d0 = 0; d0 < 3; ++d0)
-                                        sink.add(op.slot, i, j, k, d0,
-                                                 rg0 * pd[d0][0] + rg1 * pd[d0][1] + rg2 * pd[d0][2]);
-                                }
-                        break;
-                    }
+            for (int n = 0; n < NDOF; ++n) {
+                Tww[n] = fmaf(w[1][j], Sw[n], Tww[n]);
+                if (GRAD) {
+                    Tgw[n] = fmaf(g[1][j], Sw[n], Tgw[n]);
+                    Twg[n] = fmaf(w[1][j], Sg[n], Twg[n]);
                 }
             }
         }
-        __syncthreads();
-        // Flush: one atomic per touched node and dof, (sum + comp) rounded once.
-        for (int slot = 0; slot < prm.n_arrays; ++slot) {
-            const TiledArray& ta = prm.arrays[slot];
-            const int dofs = ta.a.dofs;
-            const int count = prm.box_nodes * dofs;
-            const float* sum = smem + ta.smem_offset;
-            const float* comp = sum + count;
-            for (int e = threadIdx.x; e < count; e += blockDim.x) {
-                const float v = sum[e] + comp[e];
-                if (v == 0.0f) continue;
-                const int node = e / dofs, dof = e - node * dofs;
-                const int bk = node % prm.box[2];
-                const int bj = (node / prm.box[2]) % prm.box[1];
-                const int bi = node / (prm.box[1] * prm.box[2]);
-                const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
-                if (gi >= prm.mesh.ext[0] || gj >= prm.mesh.ext[1] || gk >= prm.mesh.ext[2]) continue;
-                atomic_add_array(ta.a, node_index(prm.mesh, gi, gj, gk), dof, v);
+#pragma unroll
+        for (int n = 0; n < NDOF; ++n) {
+            V[n] = fmaf(w[0][i], Tww[n], V[n]);
+            if (GRAD) {
+                D[0][n] = fmaf(g[0][i], Tww[n], D[0][n]);
+                D[1][n] = fmaf(w[0][i], Tgw[n], D[1][n]);
+                D[2][n] = fmaf(w[0][i], Twg[n], D[2][n]);
             }
         }
-        __syncthreads();
     }
 }
 
+template <int NDOF>
+__device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, int64_t p, const float* V,
+                                          const float (*D)[3]) {
+    for (int o = 0; o < prm.n_ops; ++o) {
+        const DOp& op = prm.ops[o];
+        if (op.slot != slot) continue;
+        const float mult = float(op.mult);
+        switch (op.kind) {
+            case CGX_SCALAR_VALUE_G2P:
+                add_field<float>(op.x, p, 0, mult * V[0]);
+                break;
+            case CGX_VECTOR_VALUE_G2P:
+                if (NDOF >= 3) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) add_field<float>(op.x, p, d, mult * V[d < NDOF ? d : 0]);
+                }
+                break;
+            case CGX_SCALAR_GRADIENT_G2P:
+#pragma unroll
+                for (int d = 0; d < 3; ++d) add_field<float>(op.x, p, d, mult * D[d][0]);
+                break;
+            case CGX_VECTOR_GRADIENT_G2P:
+                if (NDOF >= 3) {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+#pragma unroll
+                        for (int b = 0; b < 3; ++b) add_field<float>(op.x, p, a * 3 + b, mult * D[a][b < NDOF ? b : 0]);
+                }
+                break;
+            case CGX_VECTOR_DIVERGENCE_G2P:
+                if (NDOF >= 3) add_field<float>(op.x, p, 0, (D[0][0] + D[1][1 < NDOF ? 1 : 0] + D[2][2 < NDOF ? 2 : 0]) * mult);
+                break;
+        }
+    }
+}
+
+// Per-slot needs, from the operators that read it.
+struct SlotNeed {
+    int ndof;   // 1 or 3
+    bool grad;
+};
+
+__device__ __forceinline__ SlotNeed slot_need(const TiledParams& prm, int slot) {
+    SlotNeed n{1, false};
+    for (int o = 0; o < prm.n_ops; ++o) {
+        if (prm.ops[o].slot != slot) continue;
+        switch (prm.ops[o].kind) {
+            case CGX_SCALAR_VALUE_G2P: break;
+            case CGX_VECTOR_VALUE_G2P: n.ndof = 3; break;
+            case CGX_SCALAR_GRADIENT_G2P: n.grad = true; break;
+            case CGX_VECTOR_GRADIENT_G2P:
+            case CGX_VECTOR_DIVERGENCE_G2P: n.ndof = 3; n.grad = true; break;
+        }
+    }
+    return n;
+}
+
+template <int ORDER, int NDOF, bool GRAD>
+__device__ __forceinline__ void gather_apply(const TiledParams& prm, int slot, const float* box, bool inbox,
+                                             const int* l, const int* s, const float (*w)[ORDER + 1],
+                                             const float (*g)[ORDER + 1], int64_t p) {
+    float V[NDOF], D[3][3];
+    gather_sums<ORDER, NDOF, GRAD>(prm, prm.arrays[slot], box, inbox, l, s, w, g, V, D);
+    apply_ops<NDOF>(prm, slot, p, V, D);
+}
+
 template <int ORDER>
-__global__ void __launch_bounds__(256) g2p_tiled_kernel(const __grid_constant__ TiledParams prm) {
-    constexpr int nk = ORDER + 1;
+__global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2) g2p_tiled_kernel(const __grid_constant__ TiledParams prm) {
+    constexpr int K = ORDER + 1;
     extern __shared__ float smem[];
     __shared__ int item_idx;
     const int64_t nwork = *prm.work_count;
@@ -239,18 +175,25 @@ __global__ void __launch_bounds__(256) g2p_tiled_kernel(const __grid_constant__ 
         if (widx >= nwork) break;
         const WorkItem it = prm.work[widx];
         int origin[3];
-        tile_origin(prm, it.tile, origin);
+        {
+            const int t2 = it.tile % prm.num_tiles[2];
+            const int t1 = (it.tile / prm.num_tiles[2]) % prm.num_tiles[1];
+            const int t0 = it.tile / (prm.num_tiles[1] * prm.num_tiles[2]);
+            origin[0] = t0 * prm.tile[0];
+            origin[1] = t1 * prm.tile[1];
+            origin[2] = t2 * prm.tile[2];
+        }
         // Stage the node box of every source array.
         for (int slot = 0; slot < prm.n_arrays; ++slot) {
             const TiledArray& ta = prm.arrays[slot];
             const int dofs = ta.a.dofs;
+            const int row = prm.box[2] * dofs;
             const int count = prm.box_nodes * dofs;
             float* dst = smem + ta.smem_offset;
             for (int e = threadIdx.x; e < count; e += blockDim.x) {
-                const int node = e / dofs, dof = e - node * dofs;
-                const int bk = node % prm.box[2];
-                const int bj = (node / prm.box[2]) % prm.box[1];
-                const int bi = node / (prm.box[1] * prm.box[2]);
+                const int r = e / row, c = e - r * row;
+                const int bj = r % prm.box[1], bi = r / prm.box[1];
+                const int bk = c / dofs, dof = c - bk * dofs;
                 const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
                 float v = 0.0f;
                 if (gi < prm.mesh.ext[0] && gj < prm.mesh.ext[1] && gk < prm.mesh.ext[2])
@@ -261,118 +204,38 @@ __global__ void __launch_bounds__(256) g2p_tiled_kernel(const __grid_constant__ 
         __syncthreads();
 
         for (int64_t p = it.begin + threadIdx.x; p < it.end; p += blockDim.x) {
+            double x[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) x[d] = load_field<double>(prm.points, p, d);
             int s[3];
-            float w[3][nk], g[3][nk];
-            if (!point_weights<ORDER>(prm, p, s, w, g)) continue;
+            float u[3];
+            if (!form_point<ORDER>(prm, x, s, u)) {
+                raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+                continue;
+            }
+            float w[3][K], g[3][K];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
             int l[3];
             bool inbox = true;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 l[d] = s[d] - origin[d];
-                inbox &= (l[d] >= 0) && (l[d] + nk <= prm.box[d]);
+                inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
             }
-            for (int o = 0; o < prm.n_ops; ++o) {
-                const DOp& op = prm.ops[o];
-                const TiledArray& ta = prm.arrays[op.slot];
-                const int dofs = ta.a.dofs;
-                const float* box = smem + ta.smem_offset;
-                auto val = [&](int i, int j, int k, int dof) -> float {
-                    if (inbox) {
-                        const int node = ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k);
-                        return box[node * dofs + dof];
-                    }
-                    return load_array<float>(ta.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), dof);
-                };
-                const float mult = float(op.mult);
-                switch (op.kind) {
-                    case CGX_SCALAR_VALUE_G2P: {
-                        float r = 0.0f;
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j)
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) r += val(i, j, k, 0) * w[0][i] * w[1][j] * w[2][k];
-                        add_field<float>(op.x, p, 0, mult * r);
-                        break;
-                    }
-                    case CGX_VECTOR_VALUE_G2P: {
-                        float r[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j) {
-                                const float wij = w[0][i] * w[1][j];
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) {
-                                    const float wijk = wij * w[2][k];
-#pragma unroll
-                                    for (int d = 0; d < 3; ++d) r[d] += val(i, j, k, d) * wijk;
-                                }
-                            }
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) add_field<float>(op.x, p, d, mult * r[d]);
-                        break;
-                    }
-                    case CGX_SCALAR_GRADIENT_G2P: {
-                        float r[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j)
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) {
-                                    const float f = val(i, j, k, 0);
-                                    r[0] += f * g[0][i] * w[1][j] * w[2][k];
-                                    r[1] += f * w[0][i] * g[1][j] * w[2][k];
-                                    r[2] += f * w[0][i] * w[1][j] * g[2][k];
-                                }
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) add_field<float>(op.x, p, d, mult * r[d]);
-                        break;
-                    }
-                    case CGX_VECTOR_GRADIENT_G2P: {
-                        float r[3][3];
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-#pragma unroll
-                            for (int b = 0; b < 3; ++b) r[a][b] = 0.0f;
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j)
-#pragma unroll
-                                for (int k = 0; k < nk; ++k) {
-                                    const float rg[3] = {g[0][i] * w[1][j] * w[2][k], w[0][i] * g[1][j] * w[2][k],
-                                                         w[0][i] * w[1][j] * g[2][k]};
-                                    float v[3];
-#pragma unroll
-                                    for (int d = 0; d < 3; ++d) v[d] = val(i, j, k, d);
-#pragma unroll
-                                    for (int a = 0; a < 3; ++a)
-#pragma unroll
-                                        for (int b = 0; b < 3; ++b) r[a][b] += rg[a] * v[b];
-                                }
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-#pragma unroll
-                            for (int b = 0; b < 3; ++b) add_field<float>(op.x, p, a * 3 + b, mult * r[a][b]);
-                        break;
-                    }
-                    case CGX_VECTOR_DIVERGENCE_G2P: {
-                        float r = 0.0f;
-#pragma unroll
-                        for (int i = 0; i < nk; ++i)
-#pragma unroll
-                            for (int j = 0; j < nk; ++j)
-#pragma unroll
-                                for (int k = 0; k < nk; ++k)
-                                    r += val(i, j, k, 0) * g[0][i] * w[1][j] * w[2][k] +
-                                         val(i, j, k, 1) * w[0][i] * g[1][j] * w[2][k] +
-                                         val(i, j, k, 2) * w[0][i] * w[1][j] * g[2][k];
-                        add_field<float>(op.x, p, 0, r * mult);
-                        break;
-                    }
+            for (int slot = 0; slot < prm.n_arrays; ++slot) {
+                const float* box = smem + prm.arrays[slot].smem_offset;
+                const SlotNeed need = slot_need(prm, slot);
+                if (need.ndof == 3) {
+                    if (need.grad)
+                        gather_apply<ORDER, 3, true>(prm, slot, box, inbox, l, s, w, g, p);
+                    else
+                        gather_apply<ORDER, 3, false>(prm, slot, box, inbox, l, s, w, g, p);
+                } else {
+                    if (need.grad)
+                        gather_apply<ORDER, 1, true>(prm, slot, box, inbox, l, s, w, g, p);
+                    else
+                        gather_apply<ORDER, 1, false>(prm, slot, box, inbox, l, s, w, g, p);
                 }
             }
         }
@@ -381,30 +244,26 @@ __global__ void __launch_bounds__(256) g2p_tiled_kernel(const __grid_constant__ 
 }
 
 template <int ORDER>
-cudaError_t launch_tiled_order(const TiledParams& prm, bool p2g, int sms, size_t smem, cudaStream_t st) {
-    const void* fn = p2g ? reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER>)
-                         : reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER>);
+cudaError_t launch_g2p_order(const TiledParams& prm, int sms, size_t smem, cudaStream_t st) {
+    const void* fn = reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    const int blocks = sms * per_sm;
-    if (p2g)
-        p2g_tiled_kernel<ORDER><<<blocks, 256, smem, st>>>(prm);
-    else
-        g2p_tiled_kernel<ORDER><<<blocks, 256, smem, st>>>(prm);
+    g2p_tiled_kernel<ORDER><<<sms * per_sm, kThreads, smem, st>>>(prm);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_tiled(const TiledParams& prm, int order, bool p2g, int sms, size_t smem, cudaStream_t st) {
+    if (p2g) return cudaErrorInvalidValue;
     switch (order) {
-        case 1: return launch_tiled_order<1>(prm, p2g, sms, smem, st);
-        case 2: return launch_tiled_order<2>(prm, p2g, sms, smem, st);
-        case 3: return launch_tiled_order<3>(prm, p2g, sms, smem, st);
+        case 1: return launch_g2p_order<1>(prm, sms, smem, st);
+        case 2: return launch_g2p_order<2>(prm, sms, smem, st);
+        case 3: return launch_g2p_order<3>(prm, sms, smem, st);
     }
     return cudaErrorInvalidValue;
 }

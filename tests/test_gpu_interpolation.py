@@ -16,7 +16,8 @@ from tests.helpers import (G2P_COMPS, G2P_DOFS, P2G_COMPS, P2G_DOFS, clumped_poi
 pytestmark = pytest.mark.gpu
 
 TOL_FP64 = 1e-12
-TOL_P2G_FP32 = 1e-6
+TOL_P2G_FP32 = 1e-6      # tiled, compensated
+TOL_P2G_FP32_POINTS = 4e-6  # point-parallel FP32 fallback: plain float atomics
 TOL_G2P_FP32 = 2e-6
 
 FORMS = [("plain64", G.PLAIN_FP64, False), ("fp32", G.FP32_COMPENSATED, False), ("fp32_tiled", G.FP32_COMPENSATED, True)]
@@ -122,7 +123,7 @@ def test_p2g_vs_oracle(oracle, form_name, precision, tiled, order, kind):
     if precision == G.FP32_COMPENSATED and order in (0, 4, 5, 6) and tiled:
         pytest.skip("tiled kernels cover orders 1-3")
     got, ref = _p2g_case(oracle, order, kind, precision, tiled, seed=100 * order + kind)
-    tol = TOL_FP64 if precision == G.PLAIN_FP64 else TOL_P2G_FP32
+    tol = TOL_FP64 if precision == G.PLAIN_FP64 else (TOL_P2G_FP32 if tiled else TOL_P2G_FP32_POINTS)
     assert max_rel(got, ref) <= tol, (form_name, order, kind, max_rel(got, ref))
 
 
