@@ -380,11 +380,19 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
             prm.work_count = reinterpret_cast<const int64_t*>(h->flags + 2);
             prm.work_counter = h->flags + 1;
             prm.error_flag = h->flags;
-            CGX_CUDA(cudaMemsetAsync(h->flags + 1, 0, sizeof(int), st));
-            if (p2g)
+            if (p2g) {
+                CGX_CUDA(cudaMemsetAsync(h->flags + 1, 0, sizeof(int), st));
                 CGX_CUDA(launch_p2g_tiled(prm, spline_order, h->sms, smem, st));
-            else
-                CGX_CUDA(launch_tiled(prm, spline_order, false, h->sms, smem, st));
+            } else {
+                // one launch per source array, its box at shared offset 0
+                for (int a = 0; a < n_arrays; ++a) {
+                    TiledParams one = prm;
+                    one.arrays[a].smem_offset = 0;
+                    const size_t smem_a = size_t(prm.box_nodes) * prm.arrays[a].a.dofs * sizeof(float);
+                    CGX_CUDA(cudaMemsetAsync(h->flags + 1, 0, sizeof(int), st));
+                    CGX_CUDA(launch_g2p_tiled(one, spline_order, a, h->sms, smem_a, st));
+                }
+            }
         }
     }
     if (!tiled && num_point > 0) {

@@ -64,6 +64,12 @@ __device__ __forceinline__ T load_field(const DField& f, int64_t p, int c) {
     return T(__ldg(reinterpret_cast<const float*>(f.data) + o));
 }
 
+// Ask the L1 to fetch the line holding element (p, c) of a field.
+__device__ __forceinline__ void prefetch_field(const DField& f, int64_t p, int c) {
+    const int64_t o = field_offset(f, p, c) * (f.dtype == CGX_F64 ? 8 : 4);
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(f.data + o));
+}
+
 template <class T>
 __device__ __forceinline__ void add_field(const DField& f, int64_t p, int c, T v) {
     const int64_t o = field_offset(f, p, c);

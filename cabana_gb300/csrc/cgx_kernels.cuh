@@ -92,7 +92,9 @@ cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64
 cudaError_t launch_halo(const HaloParams& h, bool scatter, int sms, cudaStream_t st);
 cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st);
 
-cudaError_t launch_tiled(const TiledParams& prm, int order, bool p2g, int sms, size_t smem_bytes, cudaStream_t st);
+// Tiled g2p for the operators reading array `slot` (its node box is staged at
+// shared offset 0).
+cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sms, size_t smem_bytes, cudaStream_t st);
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem_bytes, cudaStream_t st);
 // Channels per group of the tiled p2g kernel for a spline order.
 int p2g_group_capacity(int order, bool gradient);

@@ -110,43 +110,103 @@ __device__ __forceinline__ float chan_src(const TiledParams& prm, int op, int co
     return load_field<float>(o.x, p, comp) * float(o.mult);
 }
 
+template <int K>
+__device__ __forceinline__ float pick(const float* v, int idx) {
+    float r = v[0];
+#pragma unroll
+    for (int a = 1; a < K; ++a) r = (idx == a) ? v[a] : r;
+    return r;
+}
+
 // Direct (per-point) contribution of one group: compensated shared atomics
-// into the box, or global atomics when the stencil is outside the box.
+// into the box, or global atomics when the stencil is outside the box. Each
+// lane walks its stencil starting at a different node, so lanes whose points
+// share a cell do not hit the same shared address in the same instruction.
 template <int ORDER, int CH, bool GRAD>
 __device__ __forceinline__ void add_direct(const TiledParams& prm, float* smem, const ChanSmem* cs, int first,
                                            int count, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
-                                           const float (*coef)[3], bool inbox, const int* l, const int* s) {
+                                           const float (*coef)[3], bool inbox, const int* l, const int* s, int lane) {
     constexpr int K = ORDER + 1;
+    constexpr int NODES = K * K * K;
+    int node = lane % NODES;
+#pragma unroll 1
+    for (int step = 0; step < NODES; ++step) {
+        const int i = node / (K * K), j = (node / K) % K, k = node % K;
+        const float wi = pick<K>(w[0], i), wj = pick<K>(w[1], j), wk = pick<K>(w[2], k);
+        float wv = 0.0f, g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
+        if (GRAD) {
+            const float gi = pick<K>(g[0], i), gj = pick<K>(g[1], j), gk = pick<K>(g[2], k);
+            g0 = gi * wj * wk;
+            g1 = wi * gj * wk;
+            g2 = wi * wj * gk;
+        } else {
+            wv = wi * wj * wk;
+        }
+        const int bnode = inbox ? ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k) : 0;
+        const int64_t gnode = inbox ? 0 : node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            if (c >= count) break;
+            const float v = GRAD ? coef[c][0] * g0 + coef[c][1] * g1 + coef[c][2] * g2 : coef[c][0] * wv;
+            if (inbox) {
+                const ChanSmem m = cs[first + c];
+                const int e = m.sum_base + bnode * m.dofs;
+                comp_add(smem + e, smem + e + m.comp_off, v);
+            } else {
+                const Channel& ch = prm.channels[first + c];
+                atomic_add_array(prm.arrays[ch.slot].a, gnode, ch.dof, v);
+            }
+        }
+        node = (node + 1 == NODES) ? 0 : node + 1;
+    }
+}
+
+// Register accumulation of this lane's particle (zero coefficients for lanes
+// outside the current segment).
+template <int ORDER, int CH, bool GRAD, int NPAD>
+__device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
+                                           const float (*coef)[3], bool member) {
+    constexpr int K = ORDER + 1;
+    float cm[CH][3];
+#pragma unroll
+    for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int n = 0; n < 3; ++n) cm[c][n] = member ? coef[c][n] : 0.0f;
 #pragma unroll
     for (int i = 0; i < K; ++i)
 #pragma unroll
-        for (int j = 0; j < K; ++j)
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                float wv = 0.0f, g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
-                if (GRAD) {
-                    g0 = g[0][i] * w[1][j] * w[2][k];
-                    g1 = w[0][i] * g[1][j] * w[2][k];
-                    g2 = w[0][i] * w[1][j] * g[2][k];
-                } else {
-                    wv = w[0][i] * w[1][j] * w[2][k];
-                }
-                const int bnode = inbox ? ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k) : 0;
-                const int64_t gnode = inbox ? 0 : node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+        for (int j = 0; j < K; ++j) {
+            if (GRAD) {
+                const float wij = w[0][i] * w[1][j];
+                const float gi0 = g[0][i] * w[1][j];
+                const float gi1 = w[0][i] * g[1][j];
+                float P[CH], Q[CH];
 #pragma unroll
                 for (int c = 0; c < CH; ++c) {
-                    if (c >= count) break;
-                    const float v = GRAD ? coef[c][0] * g0 + coef[c][1] * g1 + coef[c][2] * g2 : coef[c][0] * wv;
-                    if (inbox) {
-                        const ChanSmem m = cs[first + c];
-                        const int e = m.sum_base + bnode * m.dofs;
-                        comp_add(smem + e, smem + e + m.comp_off, v);
-                    } else {
-                        const Channel& ch = prm.channels[first + c];
-                        atomic_add_array(prm.arrays[ch.slot].a, gnode, ch.dof, v);
-                    }
+                    P[c] = cm[c][0] * gi0 + cm[c][1] * gi1;
+                    Q[c] = cm[c][2] * wij;
                 }
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        float& a = acc[((i * K + j) * K + k) * CH + c];
+                        a = fmaf(P[c], w[2][k], fmaf(Q[c], g[2][k], a));
+                    }
+            } else {
+                const float wij = w[0][i] * w[1][j];
+                float A[CH];
+#pragma unroll
+                for (int c = 0; c < CH; ++c) A[c] = cm[c][0] * wij;
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        float& a = acc[((i * K + j) * K + k) * CH + c];
+                        a = fmaf(A[c], w[2][k], a);
+                    }
             }
+        }
 }
 
 // Reduce the warp's register sums and add them to the box.
@@ -194,16 +254,35 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* smem, c
     int cur_key = -1;
     int run_windows = 0;
 
+    // Software pipeline: coordinates of the next window are loaded, and the
+    // lines of its channel sources prefetched, while this window computes.
+    double xn[3] = {0.0, 0.0, 0.0};
+    if (b + lane < e) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, b + lane, d);
+    }
     for (int64_t w0 = b; w0 < e; w0 += 32) {
         const int64_t p = w0 + lane;
         const bool active = p < e;
+        double x[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) x[d] = xn[d];
+        const int64_t pn = p + 32;
+        if (pn < e) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, pn, d);
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                if (c >= count) break;
+                const Channel& ch = prm.channels[first + c];
+                if (ch.src_comp[0] >= 0) prefetch_field(prm.ops[ch.src_op[0]].x, pn, ch.src_comp[0]);
+                if (GRAD && ch.src_comp[2] >= 0) prefetch_field(prm.ops[ch.src_op[2]].x, pn, ch.src_comp[2]);
+            }
+        }
         int s[3] = {0, 0, 0};
         float u[3] = {0.0f, 0.0f, 0.0f};
         bool ok = false;
         if (active) {
-            double x[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) x[d] = load_field<double>(prm.points, p, d);
             ok = form_point<ORDER>(prm, x, s, u);
             if (!ok) raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
         }
@@ -215,8 +294,11 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* smem, c
             inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
         }
         const int key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : -1;
-        const int key0 = __shfl_sync(0xffffffffu, key, 0);
-        const bool uniform = __all_sync(0xffffffffu, !active || (ok && key == key0)) && key0 >= 0;
+        // Sorted particles: lanes with one key are contiguous. Count the
+        // segments of this window.
+        const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+        const unsigned starts = __ballot_sync(0xffffffffu, active && (lane == 0 || key != prev));
+        const bool all_in = __all_sync(0xffffffffu, !active || key >= 0);
 
         float w[3][K], g[3][K];
 #pragma unroll
@@ -233,56 +315,29 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* smem, c
             }
         }
 
-        if (uniform) {
-            if (key0 != cur_key || run_windows == kMaxRunWindows) {
-                if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
-                cur_key = key0;
-                run_windows = 0;
-            }
-            ++run_windows;
-            // Register accumulation; inactive lanes carry zero coefficients.
-#pragma unroll
-            for (int i = 0; i < K; ++i)
-#pragma unroll
-                for (int j = 0; j < K; ++j) {
-                    if (GRAD) {
-                        const float wij = w[0][i] * w[1][j];
-                        const float gi0 = g[0][i] * w[1][j];
-                        const float gi1 = w[0][i] * g[1][j];
-                        float P[CH], Q[CH];
-#pragma unroll
-                        for (int c = 0; c < CH; ++c) {
-                            P[c] = coef[c][0] * gi0 + coef[c][1] * gi1;
-                            Q[c] = coef[c][2] * wij;
-                        }
-#pragma unroll
-                        for (int k = 0; k < K; ++k)
-#pragma unroll
-                            for (int c = 0; c < CH; ++c) {
-                                float& a = acc[((i * K + j) * K + k) * CH + c];
-                                a = fmaf(P[c], w[2][k], fmaf(Q[c], g[2][k], a));
-                            }
-                    } else {
-                        const float wij = w[0][i] * w[1][j];
-                        float A[CH];
-#pragma unroll
-                        for (int c = 0; c < CH; ++c) A[c] = coef[c][0] * wij;
-#pragma unroll
-                        for (int k = 0; k < K; ++k)
-#pragma unroll
-                            for (int c = 0; c < CH; ++c) {
-                                float& a = acc[((i * K + j) * K + k) * CH + c];
-                                a = fmaf(A[c], w[2][k], a);
-                            }
-                    }
+        if (all_in && __popc(starts) <= 2) {
+            // One or two runs of equal base nodes: accumulate each run in
+            // registers (lanes outside it add zeros), flushing on key change.
+            unsigned rem = starts;
+            while (rem) {
+                const int sl = __ffs(rem) - 1;
+                rem &= rem - 1;
+                const int sk = __shfl_sync(0xffffffffu, key, sl);
+                if (sk != cur_key || run_windows == kMaxRunWindows) {
+                    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
+                    cur_key = sk;
+                    run_windows = 0;
                 }
+                ++run_windows;
+                accumulate<ORDER, CH, GRAD, NPAD>(acc, w, g, coef, active && key == sk);
+            }
         } else {
             if (cur_key >= 0) {
                 flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
                 cur_key = -1;
                 run_windows = 0;
             }
-            if (ok) add_direct<ORDER, CH, GRAD>(prm, smem, cs, first, count, w, g, coef, inbox, l, s);
+            if (ok) add_direct<ORDER, CH, GRAD>(prm, smem, cs, first, count, w, g, coef, inbox, l, s, lane);
         }
     }
     if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);

@@ -132,42 +132,14 @@ __device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, int6
     }
 }
 
-// Per-slot needs, from the operators that read it.
-struct SlotNeed {
-    int ndof;   // 1 or 3
-    bool grad;
-};
-
-__device__ __forceinline__ SlotNeed slot_need(const TiledParams& prm, int slot) {
-    SlotNeed n{1, false};
-    for (int o = 0; o < prm.n_ops; ++o) {
-        if (prm.ops[o].slot != slot) continue;
-        switch (prm.ops[o].kind) {
-            case CGX_SCALAR_VALUE_G2P: break;
-            case CGX_VECTOR_VALUE_G2P: n.ndof = 3; break;
-            case CGX_SCALAR_GRADIENT_G2P: n.grad = true; break;
-            case CGX_VECTOR_GRADIENT_G2P:
-            case CGX_VECTOR_DIVERGENCE_G2P: n.ndof = 3; n.grad = true; break;
-        }
-    }
-    return n;
-}
-
 template <int ORDER, int NDOF, bool GRAD>
-__device__ __forceinline__ void gather_apply(const TiledParams& prm, int slot, const float* box, bool inbox,
-                                             const int* l, const int* s, const float (*w)[ORDER + 1],
-                                             const float (*g)[ORDER + 1], int64_t p) {
-    float V[NDOF], D[3][3];
-    gather_sums<ORDER, NDOF, GRAD>(prm, prm.arrays[slot], box, inbox, l, s, w, g, V, D);
-    apply_ops<NDOF>(prm, slot, p, V, D);
-}
-
-template <int ORDER>
-__global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2) g2p_tiled_kernel(const __grid_constant__ TiledParams prm) {
+__global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2)
+    g2p_tiled_kernel(const __grid_constant__ TiledParams prm, int slot) {
     constexpr int K = ORDER + 1;
     extern __shared__ float smem[];
     __shared__ int item_idx;
     const int64_t nwork = *prm.work_count;
+    const TiledArray& ta = prm.arrays[slot];
     while (true) {
         if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
         __syncthreads();
@@ -183,13 +155,11 @@ __global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2) g2p_tiled_kernel
             origin[1] = t1 * prm.tile[1];
             origin[2] = t2 * prm.tile[2];
         }
-        // Stage the node box of every source array.
-        for (int slot = 0; slot < prm.n_arrays; ++slot) {
-            const TiledArray& ta = prm.arrays[slot];
+        // Stage the node box of the source array (coalesced rows of k * dofs).
+        {
             const int dofs = ta.a.dofs;
             const int row = prm.box[2] * dofs;
             const int count = prm.box_nodes * dofs;
-            float* dst = smem + ta.smem_offset;
             for (int e = threadIdx.x; e < count; e += blockDim.x) {
                 const int r = e / row, c = e - r * row;
                 const int bj = r % prm.box[1], bi = r / prm.box[1];
@@ -198,15 +168,36 @@ __global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2) g2p_tiled_kernel
                 float v = 0.0f;
                 if (gi < prm.mesh.ext[0] && gj < prm.mesh.ext[1] && gk < prm.mesh.ext[2])
                     v = load_array<float>(ta.a, node_index(prm.mesh, gi, gj, gk), dof);
-                dst[e] = v;
+                smem[e] = v;
             }
         }
         __syncthreads();
 
-        for (int64_t p = it.begin + threadIdx.x; p < it.end; p += blockDim.x) {
+        // Software pipeline: the next particle's coordinates are loaded and
+        // its output lines prefetched while the current one is computed.
+        double xn[3] = {0.0, 0.0, 0.0};
+        int64_t p = it.begin + threadIdx.x;
+        if (p < it.end) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, p, d);
+        }
+        for (; p < it.end; p += blockDim.x) {
             double x[3];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) x[d] = load_field<double>(prm.points, p, d);
+            for (int d = 0; d < 3; ++d) x[d] = xn[d];
+            const int64_t pn = p + blockDim.x;
+            if (pn < it.end) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, pn, d);
+                for (int o = 0; o < prm.n_ops; ++o) {
+                    if (prm.ops[o].slot != slot) continue;
+                    const int kind = prm.ops[o].kind;
+                    const int last = kind == CGX_VECTOR_GRADIENT_G2P ? 8
+                                     : (kind == CGX_VECTOR_VALUE_G2P || kind == CGX_SCALAR_GRADIENT_G2P) ? 2 : 0;
+                    prefetch_field(prm.ops[o].x, pn, 0);
+                    if (last) prefetch_field(prm.ops[o].x, pn, last);
+                }
+            }
             int s[3];
             float u[3];
             if (!form_point<ORDER>(prm, x, s, u)) {
@@ -223,47 +214,63 @@ __global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2) g2p_tiled_kernel
                 l[d] = s[d] - origin[d];
                 inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
             }
-            for (int slot = 0; slot < prm.n_arrays; ++slot) {
-                const float* box = smem + prm.arrays[slot].smem_offset;
-                const SlotNeed need = slot_need(prm, slot);
-                if (need.ndof == 3) {
-                    if (need.grad)
-                        gather_apply<ORDER, 3, true>(prm, slot, box, inbox, l, s, w, g, p);
-                    else
-                        gather_apply<ORDER, 3, false>(prm, slot, box, inbox, l, s, w, g, p);
-                } else {
-                    if (need.grad)
-                        gather_apply<ORDER, 1, true>(prm, slot, box, inbox, l, s, w, g, p);
-                    else
-                        gather_apply<ORDER, 1, false>(prm, slot, box, inbox, l, s, w, g, p);
-                }
-            }
+            float V[NDOF], D[3][3];
+            gather_sums<ORDER, NDOF, GRAD>(prm, ta, smem, inbox, l, s, w, g, V, D);
+            apply_ops<NDOF>(prm, slot, p, V, D);
         }
         __syncthreads();
     }
 }
 
-template <int ORDER>
-cudaError_t launch_g2p_order(const TiledParams& prm, int sms, size_t smem, cudaStream_t st) {
-    const void* fn = reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER>);
+template <int ORDER, int NDOF, bool GRAD>
+cudaError_t launch_g2p(const TiledParams& prm, int slot, int sms, size_t smem, cudaStream_t st) {
+    const void* fn = reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER, NDOF, GRAD>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    g2p_tiled_kernel<ORDER><<<sms * per_sm, kThreads, smem, st>>>(prm);
+    g2p_tiled_kernel<ORDER, NDOF, GRAD><<<sms * per_sm, kThreads, smem, st>>>(prm, slot);
     return cudaGetLastError();
+}
+
+template <int ORDER>
+cudaError_t launch_g2p_slot(const TiledParams& prm, int slot, int ndof, bool grad, int sms, size_t smem,
+                            cudaStream_t st) {
+    if (ndof == 3) return grad ? launch_g2p<ORDER, 3, true>(prm, slot, sms, smem, st)
+                               : launch_g2p<ORDER, 3, false>(prm, slot, sms, smem, st);
+    return grad ? launch_g2p<ORDER, 1, true>(prm, slot, sms, smem, st)
+                : launch_g2p<ORDER, 1, false>(prm, slot, sms, smem, st);
 }
 
 }  // namespace
 
-cudaError_t launch_tiled(const TiledParams& prm, int order, bool p2g, int sms, size_t smem, cudaStream_t st) {
-    if (p2g) return cudaErrorInvalidValue;
+// Dofs gathered (1 or 3) and whether gradient sums are needed, from the
+// operators that read one array.
+void g2p_slot_need(const TiledParams& prm, int slot, int& ndof, bool& grad) {
+    ndof = 1;
+    grad = false;
+    for (int o = 0; o < prm.n_ops; ++o) {
+        if (prm.ops[o].slot != slot) continue;
+        switch (prm.ops[o].kind) {
+            case CGX_SCALAR_VALUE_G2P: break;
+            case CGX_VECTOR_VALUE_G2P: ndof = 3; break;
+            case CGX_SCALAR_GRADIENT_G2P: grad = true; break;
+            case CGX_VECTOR_GRADIENT_G2P:
+            case CGX_VECTOR_DIVERGENCE_G2P: ndof = 3; grad = true; break;
+        }
+    }
+}
+
+cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sms, size_t smem, cudaStream_t st) {
+    int ndof;
+    bool grad;
+    g2p_slot_need(prm, slot, ndof, grad);
     switch (order) {
-        case 1: return launch_g2p_order<1>(prm, sms, smem, st);
-        case 2: return launch_g2p_order<2>(prm, sms, smem, st);
-        case 3: return launch_g2p_order<3>(prm, sms, smem, st);
+        case 1: return launch_g2p_slot<1>(prm, slot, ndof, grad, sms, smem, st);
+        case 2: return launch_g2p_slot<2>(prm, slot, ndof, grad, sms, smem, st);
+        case 3: return launch_g2p_slot<3>(prm, slot, ndof, grad, sms, smem, st);
     }
     return cudaErrorInvalidValue;
 }
