@@ -278,7 +278,7 @@ bool plan_channels(TiledParams& prm, const cgx_op* ops, int n_ops, int order) {
     return true;
 }
 
-constexpr int64_t kChunk = 4096;
+const int64_t kChunk = p2g_tiled_chunk();  // work-item size shared by the tiled kernels
 
 cgx_status build_work(cgx_context* h, const cgx_tiling& t, int64_t num_point, cudaStream_t st) {
     const int64_t nt = int64_t(t.num_tiles[0]) * t.num_tiles[1] * t.num_tiles[2];
@@ -372,7 +372,8 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
         for (int d = 0; d < 3; ++d) prm.c0[d] = -dm.low[d] * dm.rdx[d] + 0.5 * shift_even;
         if (p2g && !plan_channels(prm, ops, n_ops, spline_order)) tiled = false;  // too many channel groups
         const size_t smem = size_t(offset) * sizeof(float);
-        if (smem > 200 * 1024) tiled = false;  // box too large: use the point kernel
+        // box plus (for p2g) the 64 KB prep area must fit in one SM's shared memory
+        if (smem + (p2g ? 64 * 1024 : 0) > 200 * 1024) tiled = false;
         if (tiled) {
             s = build_work(h, *tiling, num_point, st);
             if (s) return s;

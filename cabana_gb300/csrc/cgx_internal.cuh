@@ -51,10 +51,14 @@ __host__ __device__ inline int first_offset(int order) {
     return (order % 2 == 0) ? -(order / 2) : -((order - 1) / 2);
 }
 
+// Element offset of (p, 0); Kokkos Views (vector length 1) take the short path.
+__device__ __forceinline__ int64_t field_base(const DField& f, int64_t p) {
+    if (f.log2vl == 0) return p * f.soa_stride;
+    return (p >> f.log2vl) * f.soa_stride + (p & ((int64_t(1) << f.log2vl) - 1));
+}
+
 __device__ __forceinline__ int64_t field_offset(const DField& f, int64_t p, int c) {
-    const int64_t s = p >> f.log2vl;
-    const int64_t a = p & ((int64_t(1) << f.log2vl) - 1);
-    return s * f.soa_stride + a + int64_t(c) * f.comp_stride;
+    return field_base(f, p) + int64_t(c) * f.comp_stride;
 }
 
 template <class T>

@@ -98,6 +98,8 @@ cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sm
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem_bytes, cudaStream_t st);
 // Channels per group of the tiled p2g kernel for a spline order.
 int p2g_group_capacity(int order, bool gradient);
+// Particles per work item of the tiled kernels.
+int64_t p2g_tiled_chunk();
 
 // Sorting / binning (cgx_sort.cu). Scratch comes from the caller.
 size_t radix_sort_scratch_bytes(int64_t n);

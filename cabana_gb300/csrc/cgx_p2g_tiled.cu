@@ -6,27 +6,30 @@
 // warp's lanes hit one address -- which is exactly what happens when the
 // particles of a warp share a cell:
 //
+//  * A work item is a tile and a contiguous run (<= 4096) of its particles.
+//    A prep pass over the item forms, once per particle, the stencil base
+//    node inside the tile's node box and the FP32 in-cell offsets (one double
+//    FMA per dimension plus integer operations) and keeps them in shared
+//    memory.
 //  * Operators are lowered to channels: one grid dof that receives, per
 //    point, a * W (value channel) or b . grad W (gradient channel). Channels
-//    are grouped (up to 4 value or 3 gradient channels per group for the
-//    quadratic spline) and each warp of the CTA takes one group, so a lane
-//    holds the group's whole stencil (27 nodes x channels) in registers.
-//  * A warp walks its run of sorted particles 32 at a time, one particle per
-//    lane. While all lanes of a window share one stencil base node, each lane
-//    adds its particle into its registers; when the base node changes the
-//    warp reduces the registers across lanes with a transpose-reduction
-//    (each lane ends with 1/32 of the sums) and adds them into the tile's
-//    shared node box with compensated atomics: one shared atomic per node
-//    and channel per run instead of one per particle.
-//  * Windows whose lanes straddle several base nodes add each particle
-//    directly (compensated shared atomics); points outside the tile's box go
-//    straight to global memory with bounds checks, so the tile ordering
-//    never changes the result.
+//    are grouped (4 value or 3 gradient channels per group for the quadratic
+//    spline) and warps are shared out among the groups in proportion to
+//    their arithmetic, so a lane holds its group's whole stencil
+//    (27 nodes x channels) in registers.
+//  * A warp walks its share of the item 32 particles at a time. While the
+//    lanes of a window hold at most two runs of equal base nodes, each lane
+//    adds its particle into its registers (lanes outside the current run add
+//    zeros); when the base node changes the warp reduces the registers across
+//    lanes with a transpose-reduction (each lane ends with 1/32 of the sums)
+//    and adds them into the box with compensated shared atomics.
+//  * Windows holding three or more runs add each particle directly with
+//    compensated shared atomics, each lane starting its stencil walk at a
+//    different node so lanes of one cell do not collide; points outside the
+//    box go to global memory with bounds checks, so the tile ordering never
+//    changes the result.
 //  * At the end of a work item the box is flushed to the Array, one atomic
 //    per touched node and dof, sum and compensation rounded once.
-//
-// The cell index and in-cell offset are formed with one double FMA per
-// dimension and integer operations; weights and products are FP32.
 #include "cgx_kernels.cuh"
 
 namespace cgx {
@@ -35,7 +38,10 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kMaxRunWindows = 16;  // register sums cover at most 16 windows per lane
+constexpr int kChunk = 4096;        // particles per work item (host builds items of this size)
+constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
+constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
+constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
 
 template <int ORDER>
 struct P2GShape {
@@ -85,17 +91,12 @@ struct ChanSmem {
     int dofs;      // node stride
 };
 
-struct PointState {
-    double x[3];
-    bool valid;
-};
-
 template <int ORDER>
-__device__ __forceinline__ bool form_point(const TiledParams& prm, const double* x, int* s, float* u) {
+__device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, int* s, float* u) {
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        const double t = fma(load_field<double>(prm.points, p, d), prm.mesh.rdx[d], prm.c0[d]);
         int c;
         ok &= split_logical(t, c, u[d]);
         s[d] = c + first_offset(ORDER);
@@ -104,10 +105,13 @@ __device__ __forceinline__ bool form_point(const TiledParams& prm, const double*
     return ok;
 }
 
-__device__ __forceinline__ float chan_src(const TiledParams& prm, int op, int comp, int64_t p) {
+__device__ __forceinline__ float load_src(const TiledParams& prm, int op, int comp, int64_t p) {
     if (comp < 0) return 0.0f;
-    const DOp& o = prm.ops[op];
-    return load_field<float>(o.x, p, comp) * float(o.mult);
+    const DField& f = prm.ops[op].x;
+    const int64_t o = field_base(f, p) + int64_t(comp) * f.comp_stride;
+    const float v = f.dtype == CGX_F64 ? float(__ldg(reinterpret_cast<const double*>(f.data) + o))
+                                       : __ldg(reinterpret_cast<const float*>(f.data) + o);
+    return v * float(prm.ops[op].mult);
 }
 
 template <int K>
@@ -120,10 +124,9 @@ __device__ __forceinline__ float pick(const float* v, int idx) {
 
 // Direct (per-point) contribution of one group: compensated shared atomics
 // into the box, or global atomics when the stencil is outside the box. Each
-// lane walks its stencil starting at a different node, so lanes whose points
-// share a cell do not hit the same shared address in the same instruction.
+// lane walks its stencil starting at a different node.
 template <int ORDER, int CH, bool GRAD>
-__device__ __forceinline__ void add_direct(const TiledParams& prm, float* smem, const ChanSmem* cs, int first,
+__device__ __forceinline__ void add_direct(const TiledParams& prm, float* box_smem, const ChanSmem* cs, int first,
                                            int count, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
                                            const float (*coef)[3], bool inbox, const int* l, const int* s, int lane) {
     constexpr int K = ORDER + 1;
@@ -151,7 +154,7 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, float* smem, 
             if (inbox) {
                 const ChanSmem m = cs[first + c];
                 const int e = m.sum_base + bnode * m.dofs;
-                comp_add(smem + e, smem + e + m.comp_off, v);
+                comp_add(box_smem + e, box_smem + e + m.comp_off, v);
             } else {
                 const Channel& ch = prm.channels[first + c];
                 atomic_add_array(prm.arrays[ch.slot].a, gnode, ch.dof, v);
@@ -162,8 +165,8 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, float* smem, 
 }
 
 // Register accumulation of this lane's particle (zero coefficients for lanes
-// outside the current segment).
-template <int ORDER, int CH, bool GRAD, int NPAD>
+// outside the current run).
+template <int ORDER, int CH, bool GRAD>
 __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
                                            const float (*coef)[3], bool member) {
     constexpr int K = ORDER + 1;
@@ -211,7 +214,7 @@ __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 
 
 // Reduce the warp's register sums and add them to the box.
 template <int ORDER, int CH, int NPAD>
-__device__ __forceinline__ void flush_run(float* acc, int lane, int key, const TiledParams& prm, float* smem,
+__device__ __forceinline__ void flush_run(float* acc, int lane, int key, const TiledParams& prm, float* box_smem,
                                           const ChanSmem* cs, int first, int count) {
     constexpr int K = ORDER + 1;
     constexpr int NODES = K * K * K;
@@ -230,21 +233,24 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
             const int bnode = ((l0 + i) * prm.box[1] + (l1 + j)) * prm.box[2] + (l2 + k);
             const ChanSmem m = cs[first + c];
             const int e = m.sum_base + bnode * m.dofs;
-            comp_add(smem + e, smem + e + m.comp_off, acc[r]);
+            comp_add(box_smem + e, box_smem + e + m.comp_off, acc[r]);
         }
     }
 #pragma unroll
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
 }
 
-// One warp processes particles [b, e) of the current work item for one group.
+// One warp processes item-local particles [b, e) for channel group gi.
+// prep[i] = (u0, u1, u2, key) of item particle i.
 template <int ORDER, bool GRAD>
-__device__ __forceinline__ void run_group(const TiledParams& prm, float* smem, const ChanSmem* cs, int gi,
-                                          const int* origin, int64_t b, int64_t e, int lane) {
+__device__ __forceinline__ void run_group(const TiledParams& prm, float* box_smem, const float4* prep,
+                                          const ChanSmem* cs, int gi, const int* origin, int64_t item_begin, int b,
+                                          int e, int lane) {
     using SH = P2GShape<ORDER>;
     constexpr int K = SH::K;
     constexpr int CH = GRAD ? SH::CG : SH::CV;
     constexpr int NPAD = GRAD ? SH::NG : SH::NV;
+    constexpr int NS = GRAD ? 3 : 1;  // sources per channel
     const ChannelGroup grp = prm.groups[gi];
     const int first = grp.first, count = grp.count;
 
@@ -254,100 +260,99 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* smem, c
     int cur_key = -1;
     int run_windows = 0;
 
-    // Software pipeline: coordinates of the next window are loaded, and the
-    // lines of its channel sources prefetched, while this window computes.
-    double xn[3] = {0.0, 0.0, 0.0};
-    if (b + lane < e) {
+    // Sources of the next window are loaded one window ahead.
+    float src_next[CH][NS];
+    {
+        const int i = b + lane;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, b + lane, d);
+        for (int c = 0; c < CH; ++c) {
+            const Channel& ch = prm.channels[first + (c < count ? c : 0)];
+#pragma unroll
+            for (int n = 0; n < NS; ++n)
+                src_next[c][n] = (i < e && c < count) ? load_src(prm, ch.src_op[n], ch.src_comp[n], item_begin + i) : 0.0f;
+        }
     }
-    for (int64_t w0 = b; w0 < e; w0 += 32) {
-        const int64_t p = w0 + lane;
-        const bool active = p < e;
-        double x[3];
+
+    for (int w0 = b; w0 < e; w0 += 32) {
+        const int i = w0 + lane;
+        const bool active = i < e;
+        float coef[CH][3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) x[d] = xn[d];
-        const int64_t pn = p + 32;
-        if (pn < e) {
+        for (int c = 0; c < CH; ++c)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, pn, d);
+            for (int n = 0; n < 3; ++n) coef[c][n] = n < NS ? src_next[c][n < NS ? n : 0] : 0.0f;
+        if (w0 + 32 < e) {
+            const int in = i + 32;
 #pragma unroll
             for (int c = 0; c < CH; ++c) {
-                if (c >= count) break;
-                const Channel& ch = prm.channels[first + c];
-                if (ch.src_comp[0] >= 0) prefetch_field(prm.ops[ch.src_op[0]].x, pn, ch.src_comp[0]);
-                if (GRAD && ch.src_comp[2] >= 0) prefetch_field(prm.ops[ch.src_op[2]].x, pn, ch.src_comp[2]);
+                const Channel& ch = prm.channels[first + (c < count ? c : 0)];
+#pragma unroll
+                for (int n = 0; n < NS; ++n)
+                    src_next[c][n] =
+                        (in < e && c < count) ? load_src(prm, ch.src_op[n], ch.src_comp[n], item_begin + in) : 0.0f;
             }
         }
-        int s[3] = {0, 0, 0};
-        float u[3] = {0.0f, 0.0f, 0.0f};
-        bool ok = false;
-        if (active) {
-            ok = form_point<ORDER>(prm, x, s, u);
-            if (!ok) raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
-        }
-        int l[3];
-        bool inbox = ok;
+        float4 pu = active ? prep[i] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kKeyInvalid));
+        const int key = __float_as_int(pu.w);
+        const float u[3] = {pu.x, pu.y, pu.z};
+        float w[3][K], g[3][K];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            l[d] = s[d] - origin[d];
-            inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
-        }
-        const int key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : -1;
-        // Sorted particles: lanes with one key are contiguous. Count the
-        // segments of this window.
+        for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+
+        // Sorted particles: lanes with one key are contiguous.
         const int prev = __shfl_up_sync(0xffffffffu, key, 1);
         const unsigned starts = __ballot_sync(0xffffffffu, active && (lane == 0 || key != prev));
         const bool all_in = __all_sync(0xffffffffu, !active || key >= 0);
 
-        float w[3][K], g[3][K];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
-        float coef[CH][3];
-#pragma unroll
-        for (int c = 0; c < CH; ++c) {
-            const bool use = ok && c < count;
-            const Channel& ch = prm.channels[first + (c < count ? c : 0)];
-#pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                coef[c][n] = 0.0f;
-                if (n == 0 || GRAD) coef[c][n] = use ? chan_src(prm, ch.src_op[n], ch.src_comp[n], p) : 0.0f;
-            }
-        }
-
         if (all_in && __popc(starts) <= 2) {
-            // One or two runs of equal base nodes: accumulate each run in
-            // registers (lanes outside it add zeros), flushing on key change.
             unsigned rem = starts;
             while (rem) {
                 const int sl = __ffs(rem) - 1;
                 rem &= rem - 1;
                 const int sk = __shfl_sync(0xffffffffu, key, sl);
                 if (sk != cur_key || run_windows == kMaxRunWindows) {
-                    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
+                    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
                     cur_key = sk;
                     run_windows = 0;
                 }
                 ++run_windows;
-                accumulate<ORDER, CH, GRAD, NPAD>(acc, w, g, coef, active && key == sk);
+                accumulate<ORDER, CH, GRAD>(acc, w, g, coef, active && key == sk);
             }
         } else {
             if (cur_key >= 0) {
-                flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
+                flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
                 cur_key = -1;
                 run_windows = 0;
             }
-            if (ok) add_direct<ORDER, CH, GRAD>(prm, smem, cs, first, count, w, g, coef, inbox, l, s, lane);
+            if (active && key != kKeyInvalid) {
+                int l[3], s[3];
+                bool inbox = key >= 0;
+                if (inbox) {
+                    l[2] = key % prm.box[2];
+                    l[1] = (key / prm.box[2]) % prm.box[1];
+                    l[0] = key / (prm.box[1] * prm.box[2]);
+                    for (int d = 0; d < 3; ++d) s[d] = origin[d] + l[d];
+                } else {
+                    float uu[3];
+                    form_point<ORDER>(prm, item_begin + i, s, uu);
+                }
+                add_direct<ORDER, CH, GRAD>(prm, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
+            }
         }
     }
-    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, smem, cs, first, count);
+    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
 }
 
 template <int ORDER>
 __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_constant__ TiledParams prm) {
-    extern __shared__ float smem[];
+    using SH = P2GShape<ORDER>;
+    constexpr int K = ORDER + 1;
+    extern __shared__ __align__(16) float smem[];
+    float* box_smem = smem;
+    float4* prep = reinterpret_cast<float4*>(smem + ((prm.smem_floats + 3) & ~3));
     __shared__ ChanSmem cs[kMaxChannels];
     __shared__ int item_idx;
+    __shared__ int warp_group[kWarps], warp_rank[kWarps], group_warps[kMaxGroups];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int c = threadIdx.x; c < prm.n_channels; c += blockDim.x) {
         const Channel ch = prm.channels[c];
@@ -356,16 +361,40 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         cs[c].comp_off = prm.box_nodes * ta.a.dofs;
         cs[c].dofs = ta.a.dofs;
     }
-    const int64_t nwork = *prm.work_count;
     const int ng = prm.n_groups;
-    const int wpg = ng <= kWarps ? kWarps / ng : 1;  // warps per group
+    if (threadIdx.x == 0) {
+        // Share the warps among the groups in proportion to their arithmetic
+        // (a gradient channel costs about twice a value channel).
+        int cost[kMaxGroups], total = 0;
+        for (int gi = 0; gi < ng; ++gi) {
+            cost[gi] = prm.groups[gi].count * (prm.groups[gi].gradient ? 2 * SH::CV / SH::CG : 1);
+            total += cost[gi];
+            group_warps[gi] = 1;
+        }
+        for (int left = kWarps - ng; left > 0 && ng > 0; --left) {
+            int best = 0;
+            for (int gi = 1; gi < ng; ++gi)
+                if (cost[gi] * group_warps[best] > cost[best] * group_warps[gi]) best = gi;
+            group_warps[best] += 1;
+        }
+        (void)total;
+        int w = 0;
+        for (int gi = 0; gi < ng && w < kWarps; ++gi)
+            for (int r = 0; r < group_warps[gi] && w < kWarps; ++r, ++w) {
+                warp_group[w] = gi;
+                warp_rank[w] = r;
+            }
+        for (; w < kWarps; ++w) warp_group[w] = -1;
+    }
+    const int64_t nwork = *prm.work_count;
     while (true) {
         if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
-        for (int i = threadIdx.x; i < prm.smem_floats; i += blockDim.x) smem[i] = 0.0f;
+        for (int i = threadIdx.x; i < prm.smem_floats; i += blockDim.x) box_smem[i] = 0.0f;
         __syncthreads();
         const int64_t widx = item_idx;
         if (widx >= nwork) break;
         const WorkItem it = prm.work[widx];
+        const int len = int(it.end - it.begin);
         int origin[3];
         {
             const int t2 = it.tile % prm.num_tiles[2];
@@ -375,27 +404,47 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             origin[1] = t1 * prm.tile[1];
             origin[2] = t2 * prm.tile[2];
         }
+        // Prep: base node key in the box and in-cell offsets, once per particle.
+        for (int i = threadIdx.x; i < len; i += blockDim.x) {
+            int s[3];
+            float u[3];
+            int key;
+            if (!form_point<ORDER>(prm, it.begin + i, s, u)) {
+                raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+                key = kKeyInvalid;
+            } else {
+                int l[3];
+                bool inbox = true;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    l[d] = s[d] - origin[d];
+                    inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
+                }
+                key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : kKeyOutside;
+            }
+            prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
+        }
+        __syncthreads();
         if (ng <= kWarps) {
-            const int gi = warp / wpg;
-            if (gi < ng) {
-                const int r = warp % wpg;
-                const int64_t len = it.end - it.begin;
-                const int64_t per = ((len + wpg - 1) / wpg + 31) / 32 * 32;
-                const int64_t b = it.begin + r * per;
-                const int64_t e = (b + per < it.end) ? b + per : it.end;
+            const int gi = warp_group[warp];
+            if (gi >= 0) {
+                const int wpg = group_warps[gi], r = warp_rank[warp];
+                const int per = ((len + wpg - 1) / wpg + 31) / 32 * 32;
+                const int b = r * per;
+                const int e = (b + per < len) ? b + per : len;
                 if (b < e) {
                     if (prm.groups[gi].gradient)
-                        run_group<ORDER, true>(prm, smem, cs, gi, origin, b, e, lane);
+                        run_group<ORDER, true>(prm, box_smem, prep, cs, gi, origin, it.begin, b, e, lane);
                     else
-                        run_group<ORDER, false>(prm, smem, cs, gi, origin, b, e, lane);
+                        run_group<ORDER, false>(prm, box_smem, prep, cs, gi, origin, it.begin, b, e, lane);
                 }
             }
         } else {
             for (int gi = warp; gi < ng; gi += kWarps) {
                 if (prm.groups[gi].gradient)
-                    run_group<ORDER, true>(prm, smem, cs, gi, origin, it.begin, it.end, lane);
+                    run_group<ORDER, true>(prm, box_smem, prep, cs, gi, origin, it.begin, 0, len, lane);
                 else
-                    run_group<ORDER, false>(prm, smem, cs, gi, origin, it.begin, it.end, lane);
+                    run_group<ORDER, false>(prm, box_smem, prep, cs, gi, origin, it.begin, 0, len, lane);
             }
         }
         __syncthreads();
@@ -404,7 +453,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             const TiledArray& ta = prm.arrays[slot];
             const int dofs = ta.a.dofs;
             const int count = prm.box_nodes * dofs;
-            const float* sum = smem + ta.smem_offset;
+            const float* sum = box_smem + ta.smem_offset;
             const float* comp = sum + count;
             for (int e = threadIdx.x; e < count; e += blockDim.x) {
                 const float v = sum[e] + comp[e];
@@ -423,7 +472,8 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
 }
 
 template <int ORDER>
-cudaError_t launch_order(const TiledParams& prm, int sms, size_t smem, cudaStream_t st) {
+cudaError_t launch_order(const TiledParams& prm, int sms, size_t box_bytes, cudaStream_t st) {
+    const size_t smem = (box_bytes + 15) / 16 * 16 + size_t(kChunk) * sizeof(float4);
     const void* fn = reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -445,6 +495,8 @@ int p2g_group_capacity(int order, bool gradient) {
     }
     return 0;
 }
+
+int64_t p2g_tiled_chunk() { return kChunk; }
 
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem, cudaStream_t st) {
     switch (order) {

@@ -35,8 +35,8 @@ __device__ __forceinline__ bool form_point(const TiledParams& prm, const double*
 }
 
 // Gather sums for one array: V[n] = sum W v_n, D[m][n] = sum d_m W v_n.
-template <int ORDER, int NDOF, bool GRAD>
-__device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledArray& ta, const float* box, bool inbox,
+template <int ORDER, int NDOF, bool GRAD, bool BOXED>
+__device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledArray& ta, const float* box,
                                             const int* l, const int* s, const float (*w)[ORDER + 1],
                                             const float (*g)[ORDER + 1], float* V, float (*D)[3]) {
     constexpr int K = ORDER + 1;
@@ -60,7 +60,7 @@ __device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledA
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 float v[NDOF];
-                if (inbox) {
+                if (BOXED) {
                     const int node = ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k);
 #pragma unroll
                     for (int n = 0; n < NDOF; ++n) v[n] = box[node * dofs + n];
@@ -215,7 +215,10 @@ __global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2)
                 inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
             }
             float V[NDOF], D[3][3];
-            gather_sums<ORDER, NDOF, GRAD>(prm, ta, smem, inbox, l, s, w, g, V, D);
+            if (inbox)
+                gather_sums<ORDER, NDOF, GRAD, true>(prm, ta, smem, l, s, w, g, V, D);
+            else
+                gather_sums<ORDER, NDOF, GRAD, false>(prm, ta, smem, l, s, w, g, V, D);
             apply_ops<NDOF>(prm, slot, p, V, D);
         }
         __syncthreads();
