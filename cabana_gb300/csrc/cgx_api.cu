@@ -209,13 +209,29 @@ cgx_status halo_all(const cgx_mesh& m, const cgx_op* ops, int n_ops, bool scatte
 bool plan_channels(TiledParams& prm, const cgx_op* ops, int n_ops, int order) {
     Channel val[kMaxChannels], grd[kMaxChannels];
     int nv = 0, ng = 0;
+    int nsrc = 0;
+    bool too_many = false;
+    auto source = [&](int op, int comp) -> int8_t {
+        if (comp < 0) return -1;
+        for (int s = 0; s < nsrc; ++s)
+            if (prm.sources[s].op == op && prm.sources[s].comp == comp) return int8_t(s);
+        if (nsrc == kMaxSources) {
+            too_many = true;
+            return -1;
+        }
+        prm.sources[nsrc].op = int8_t(op);
+        prm.sources[nsrc].comp = int8_t(comp);
+        prm.sources[nsrc].reserved = 0;
+        prm.sources[nsrc].mult = float(prm.ops[op].mult);
+        return int8_t(nsrc++);
+    };
     auto add = [&](bool gradient, int slot, int dof, int op, const int* comps) {
         Channel c;
         c.slot = int8_t(slot);
         c.dof = int8_t(dof);
         for (int n = 0; n < 3; ++n) {
-            c.src_op[n] = int8_t(op);
-            c.src_comp[n] = int8_t(comps[n]);
+            c.src[n] = source(op, comps[n]);
+            c.reserved[n] = 0;
         }
         if (gradient)
             grd[ng++] = c;
@@ -273,6 +289,8 @@ bool plan_channels(TiledParams& prm, const cgx_op* ops, int n_ops, int order) {
         ++g;
     }
     for (int i = 0; i < ng; ++i) prm.channels[n++] = grd[i];
+    if (too_many) return false;
+    prm.n_sources = nsrc;
     prm.n_channels = n;
     prm.n_groups = g;
     return true;
@@ -363,6 +381,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
             prm.ops[o].kind = ops[o].kind;
             prm.ops[o].slot = slot;
             prm.ops[o].mult = ops[o].multiplier;
+            prm.ops[o].mult_f = float(ops[o].multiplier);
             prm.ops[o].x = to_dfield(ops[o].x);
             prm.ops[o].a = prm.arrays[slot].a;
         }
@@ -372,8 +391,13 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
         for (int d = 0; d < 3; ++d) prm.c0[d] = -dm.low[d] * dm.rdx[d] + 0.5 * shift_even;
         if (p2g && !plan_channels(prm, ops, n_ops, spline_order)) tiled = false;  // too many channel groups
         const size_t smem = size_t(offset) * sizeof(float);
-        // box plus (for p2g) the 64 KB prep area must fit in one SM's shared memory
-        if (smem + (p2g ? 64 * 1024 : 0) > 200 * 1024) tiled = false;
+        // node boxes plus per-item staging must fit in one SM's shared memory
+        if (p2g) {
+            if (p2g_tiled_smem(prm, smem) > 220 * 1024) tiled = false;
+        } else {
+            for (int a = 0; a < n_arrays; ++a)
+                if (g2p_tiled_smem(prm, a) > 220 * 1024) tiled = false;
+        }
         if (tiled) {
             s = build_work(h, *tiling, num_point, st);
             if (s) return s;
@@ -389,7 +413,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
                 for (int a = 0; a < n_arrays; ++a) {
                     TiledParams one = prm;
                     one.arrays[a].smem_offset = 0;
-                    const size_t smem_a = size_t(prm.box_nodes) * prm.arrays[a].a.dofs * sizeof(float);
+                    const size_t smem_a = g2p_tiled_smem(prm, a);
                     CGX_CUDA(cudaMemsetAsync(h->flags + 1, 0, sizeof(int), st));
                     CGX_CUDA(launch_g2p_tiled(one, spline_order, a, h->sms, smem_a, st));
                 }
@@ -408,6 +432,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
             prm.ops[o].kind = ops[o].kind;
             prm.ops[o].slot = o;
             prm.ops[o].mult = ops[o].multiplier;
+            prm.ops[o].mult_f = float(ops[o].multiplier);
             prm.ops[o].x = to_dfield(ops[o].x);
             prm.ops[o].a.data = reinterpret_cast<char*>(ops[o].array.data);
             prm.ops[o].a.dtype = ops[o].array.dtype;

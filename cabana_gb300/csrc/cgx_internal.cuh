@@ -32,6 +32,8 @@ struct DOp {
     int32_t kind;
     int32_t slot;  // index of the distinct target array (tiled kernels)
     double mult;
+    float mult_f;  // the multiplier rounded to FP32 once, on the host
+    int32_t reserved;
     DField x;
     DArray a;
 };

@@ -44,13 +44,24 @@ struct WorkItem {
 
 // One accumulation channel of a tiled p2g launch: a dof of a target array
 // that receives, per point, either a * W (value channel) or b . grad W
-// (gradient channel). Sources name (op, component); comp < 0 means zero.
+// (gradient channel). src[] index the source table; -1 means zero.
 struct Channel {
     int8_t slot;
     int8_t dof;
-    int8_t src_op[3];
-    int8_t src_comp[3];
+    int8_t src[3];
+    int8_t reserved[3];
 };
+
+// A per-point input value of a tiled p2g launch: component `comp` of the
+// field of operator `op`, times the operator's multiplier.
+struct Source {
+    int8_t op;
+    int8_t comp;
+    int16_t reserved;
+    float mult;
+};
+
+constexpr int kMaxSources = 16;
 
 // A set of channels processed together by one warp role.
 struct ChannelGroup {
@@ -84,8 +95,11 @@ struct TiledParams {
     TiledArray arrays[kMaxOps];
     int32_t n_channels;
     int32_t n_groups;
+    int32_t n_sources;
+    int32_t reserved2;
     Channel channels[kMaxChannels];
     ChannelGroup groups[kMaxGroups];
+    Source sources[kMaxSources];
 };
 
 cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64, int sms, cudaStream_t st);
@@ -98,8 +112,14 @@ cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sm
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem_bytes, cudaStream_t st);
 // Channels per group of the tiled p2g kernel for a spline order.
 int p2g_group_capacity(int order, bool gradient);
+// Dynamic shared memory of the tiled g2p kernel for array `slot` (huge when
+// the launch cannot be tiled: double point fields or too many components).
+size_t g2p_tiled_smem(const TiledParams& prm, int slot);
 // Particles per work item of the tiled kernels.
 int64_t p2g_tiled_chunk();
+// Dynamic shared memory of the tiled p2g kernel: node boxes + per-item
+// staging of base keys, offsets and sources.
+size_t p2g_tiled_smem(const TiledParams& prm, size_t box_bytes);
 
 // Sorting / binning (cgx_sort.cu). Scratch comes from the caller.
 size_t radix_sort_scratch_bytes(int64_t n);

@@ -38,7 +38,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kChunk = 4096;        // particles per work item (host builds items of this size)
+constexpr int kChunk = 2048;        // particles per work item (host builds items of this size)
 constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
@@ -105,13 +105,12 @@ __device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, in
     return ok;
 }
 
-__device__ __forceinline__ float load_src(const TiledParams& prm, int op, int comp, int64_t p) {
-    if (comp < 0) return 0.0f;
-    const DField& f = prm.ops[op].x;
-    const int64_t o = field_base(f, p) + int64_t(comp) * f.comp_stride;
+__device__ __forceinline__ float load_src(const TiledParams& prm, const Source& src, int64_t p) {
+    const DField& f = prm.ops[src.op].x;
+    const int64_t o = field_base(f, p) + int64_t(src.comp) * f.comp_stride;
     const float v = f.dtype == CGX_F64 ? float(__ldg(reinterpret_cast<const double*>(f.data) + o))
                                        : __ldg(reinterpret_cast<const float*>(f.data) + o);
-    return v * float(prm.ops[op].mult);
+    return v * src.mult;
 }
 
 template <int K>
@@ -241,11 +240,12 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
 }
 
 // One warp processes item-local particles [b, e) for channel group gi.
-// prep[i] = (u0, u1, u2, key) of item particle i.
+// prep[i] = (u0, u1, u2, key) of item particle i; srcs[s * kChunk + i] is
+// source s of item particle i (multiplier applied).
 template <int ORDER, bool GRAD>
 __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_smem, const float4* prep,
-                                          const ChanSmem* cs, int gi, const int* origin, int64_t item_begin, int b,
-                                          int e, int lane) {
+                                          const float* srcs, const ChanSmem* cs, int gi, const int* origin,
+                                          int64_t item_begin, int b, int e, int lane) {
     using SH = P2GShape<ORDER>;
     constexpr int K = SH::K;
     constexpr int CH = GRAD ? SH::CG : SH::CV;
@@ -253,25 +253,18 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
     constexpr int NS = GRAD ? 3 : 1;  // sources per channel
     const ChannelGroup grp = prm.groups[gi];
     const int first = grp.first, count = grp.count;
+    // Shared-memory rows of this group's sources (-1: zero).
+    int srow[CH][NS];
+#pragma unroll
+    for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int n = 0; n < NS; ++n) srow[c][n] = c < count ? prm.channels[first + c].src[n] : -1;
 
     float acc[NPAD];
 #pragma unroll
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
     int cur_key = -1;
     int run_windows = 0;
-
-    // Sources of the next window are loaded one window ahead.
-    float src_next[CH][NS];
-    {
-        const int i = b + lane;
-#pragma unroll
-        for (int c = 0; c < CH; ++c) {
-            const Channel& ch = prm.channels[first + (c < count ? c : 0)];
-#pragma unroll
-            for (int n = 0; n < NS; ++n)
-                src_next[c][n] = (i < e && c < count) ? load_src(prm, ch.src_op[n], ch.src_comp[n], item_begin + i) : 0.0f;
-        }
-    }
 
     for (int w0 = b; w0 < e; w0 += 32) {
         const int i = w0 + lane;
@@ -280,18 +273,10 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
 #pragma unroll
         for (int c = 0; c < CH; ++c)
 #pragma unroll
-            for (int n = 0; n < 3; ++n) coef[c][n] = n < NS ? src_next[c][n < NS ? n : 0] : 0.0f;
-        if (w0 + 32 < e) {
-            const int in = i + 32;
-#pragma unroll
-            for (int c = 0; c < CH; ++c) {
-                const Channel& ch = prm.channels[first + (c < count ? c : 0)];
-#pragma unroll
-                for (int n = 0; n < NS; ++n)
-                    src_next[c][n] =
-                        (in < e && c < count) ? load_src(prm, ch.src_op[n], ch.src_comp[n], item_begin + in) : 0.0f;
+            for (int n = 0; n < 3; ++n) {
+                const int r = n < NS ? srow[c][n < NS ? n : 0] : -1;
+                coef[c][n] = (r >= 0 && active) ? srcs[r * kChunk + i] : 0.0f;
             }
-        }
         float4 pu = active ? prep[i] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kKeyInvalid));
         const int key = __float_as_int(pu.w);
         const float u[3] = {pu.x, pu.y, pu.z};
@@ -350,6 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     extern __shared__ __align__(16) float smem[];
     float* box_smem = smem;
     float4* prep = reinterpret_cast<float4*>(smem + ((prm.smem_floats + 3) & ~3));
+    float* srcs = reinterpret_cast<float*>(prep + kChunk);
     __shared__ ChanSmem cs[kMaxChannels];
     __shared__ int item_idx;
     __shared__ int warp_group[kWarps], warp_rank[kWarps], group_warps[kMaxGroups];
@@ -423,6 +409,8 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : kKeyOutside;
             }
             prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
+            for (int sidx = 0; sidx < prm.n_sources; ++sidx)
+                srcs[sidx * kChunk + i] = load_src(prm, prm.sources[sidx], it.begin + i);
         }
         __syncthreads();
         if (ng <= kWarps) {
@@ -434,17 +422,17 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int e = (b + per < len) ? b + per : len;
                 if (b < e) {
                     if (prm.groups[gi].gradient)
-                        run_group<ORDER, true>(prm, box_smem, prep, cs, gi, origin, it.begin, b, e, lane);
+                        run_group<ORDER, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
                     else
-                        run_group<ORDER, false>(prm, box_smem, prep, cs, gi, origin, it.begin, b, e, lane);
+                        run_group<ORDER, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
                 }
             }
         } else {
             for (int gi = warp; gi < ng; gi += kWarps) {
                 if (prm.groups[gi].gradient)
-                    run_group<ORDER, true>(prm, box_smem, prep, cs, gi, origin, it.begin, 0, len, lane);
+                    run_group<ORDER, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
                 else
-                    run_group<ORDER, false>(prm, box_smem, prep, cs, gi, origin, it.begin, 0, len, lane);
+                    run_group<ORDER, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
             }
         }
         __syncthreads();
@@ -471,9 +459,13 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     }
 }
 
+size_t smem_bytes(const TiledParams& prm, size_t box_bytes) {
+    return (box_bytes + 15) / 16 * 16 + size_t(kChunk) * sizeof(float4) + size_t(prm.n_sources) * kChunk * sizeof(float);
+}
+
 template <int ORDER>
 cudaError_t launch_order(const TiledParams& prm, int sms, size_t box_bytes, cudaStream_t st) {
-    const size_t smem = (box_bytes + 15) / 16 * 16 + size_t(kChunk) * sizeof(float4);
+    const size_t smem = smem_bytes(prm, box_bytes);
     const void* fn = reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -497,6 +489,8 @@ int p2g_group_capacity(int order, bool gradient) {
 }
 
 int64_t p2g_tiled_chunk() { return kChunk; }
+
+size_t p2g_tiled_smem(const TiledParams& prm, size_t box_bytes) { return smem_bytes(prm, box_bytes); }
 
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem, cudaStream_t st) {
     switch (order) {

@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) p2g_points_kernel(const __grid_constant__
         }
         for (int o = 0; o < prm.n_ops; ++o) {
             const DOp& op = prm.ops[o];
-            const T mult = T(op.mult);
+            const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
             switch (op.kind) {
                 case CGX_SCALAR_VALUE_P2G: {
                     const T pd = load_field<T>(op.x, p, 0) * mult;
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256) g2p_points_kernel(const __grid_constant__
         }
         for (int o = 0; o < prm.n_ops; ++o) {
             const DOp& op = prm.ops[o];
-            const T mult = T(op.mult);
+            const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
             switch (op.kind) {
                 case CGX_SCALAR_VALUE_G2P: {
                     T result = T(0);

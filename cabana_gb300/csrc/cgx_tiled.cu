@@ -1,15 +1,23 @@
 // Tiled grid-to-point for particles in tile-major order (FP32 form).
 //
 // A persistent grid pulls work items (a tile and a contiguous run of its
-// particles) from a device counter. The CTA stages the tile's node box of
-// every source array in shared memory with coalesced loads, then each thread
-// gathers for one particle at a time. All operators that read one array share
-// a single pass over the stencil that forms, per dof n, the value sum
-// V_n = sum W v_n and the gradient sums D_mn = sum d_m W v_n in factorised
-// (tensor-product) order; each functor then takes its result from them:
-//   ScalarValueG2P V_0, VectorValueG2P V_n, ScalarGradientG2P D_m0,
-//   VectorGradientG2P D_mn, VectorDivergenceG2P sum_m D_mm
-// (grid/src/Cabana_Grid_Interpolation.hpp:53-364, :938-1182).
+// particles) from a device counter and handles them in three passes over
+// sub-runs of up to 1024 particles, so that global memory is touched only in
+// long runs of independent loads and stores:
+//   1. load: the coordinates are read and turned into the stencil base node
+//      inside the tile's node box and FP32 in-cell offsets (one double FMA per
+//      dimension plus integer operations); the current values of the point
+//      fields being accumulated are copied into shared memory;
+//   2. compute: each thread gathers for one particle from the node box staged
+//      in shared memory. All operators that read the array share one pass
+//      over the stencil that forms, per dof n, the value sum V_n = sum W v_n
+//      and the gradient sums D_mn = sum d_m W v_n in factorised
+//      (tensor-product) order; each functor takes its result from them:
+//        ScalarValueG2P V_0, VectorValueG2P V_n, ScalarGradientG2P D_m0,
+//        VectorGradientG2P D_mn, VectorDivergenceG2P sum_m D_mm
+//      (grid/src/Cabana_Grid_Interpolation.hpp:53-364, :938-1182), and adds
+//      multiplier * result to the staged field values;
+//   3. store: the staged field values are written back.
 // A point whose stencil leaves the box reads the Array directly, so the
 // ordering never changes the result.
 #include "cgx_kernels.cuh"
@@ -19,13 +27,31 @@ namespace cgx {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kSub = 1024;          // particles per pass
+constexpr int kMaxOutCols = 24;     // staged point-field components per launch
+constexpr int kKeyOutside = -1;
+constexpr int kKeyInvalid = -2;
+
+int g2p_comps(int kind) {
+    switch (kind) {
+        case CGX_SCALAR_VALUE_G2P: case CGX_VECTOR_DIVERGENCE_G2P: return 1;
+        case CGX_VECTOR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 3;
+        case CGX_VECTOR_GRADIENT_G2P: return 9;
+    }
+    return 0;
+}
+
+__device__ __forceinline__ int dev_g2p_comps(int kind) {
+    return kind == CGX_VECTOR_GRADIENT_G2P ? 9
+           : (kind == CGX_VECTOR_VALUE_G2P || kind == CGX_SCALAR_GRADIENT_G2P) ? 3 : 1;
+}
 
 template <int ORDER>
-__device__ __forceinline__ bool form_point(const TiledParams& prm, const double* x, int* s, float* u) {
+__device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, int* s, float* u) {
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        const double t = fma(load_field<double>(prm.points, p, d), prm.mesh.rdx[d], prm.c0[d]);
         int c;
         ok &= split_logical(t, c, u[d]);
         s[d] = c + first_offset(ORDER);
@@ -96,50 +122,59 @@ __device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledA
     }
 }
 
+// Adds multiplier * result of every operator of this launch into the staged
+// point-field values (out[col * kSub + i]).
 template <int NDOF>
-__device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, int64_t p, const float* V,
+__device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, float* out, int i, const float* V,
                                           const float (*D)[3]) {
+    int col = 0;
     for (int o = 0; o < prm.n_ops; ++o) {
         const DOp& op = prm.ops[o];
         if (op.slot != slot) continue;
-        const float mult = float(op.mult);
+        const float mult = op.mult_f;
+        float* x = out + col * kSub + i;
         switch (op.kind) {
             case CGX_SCALAR_VALUE_G2P:
-                add_field<float>(op.x, p, 0, mult * V[0]);
+                x[0] += mult * V[0];
+                col += 1;
                 break;
             case CGX_VECTOR_VALUE_G2P:
-                if (NDOF >= 3) {
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) add_field<float>(op.x, p, d, mult * V[d < NDOF ? d : 0]);
-                }
+                for (int d = 0; d < 3; ++d) x[d * kSub] += mult * V[d < NDOF ? d : 0];
+                col += 3;
                 break;
             case CGX_SCALAR_GRADIENT_G2P:
 #pragma unroll
-                for (int d = 0; d < 3; ++d) add_field<float>(op.x, p, d, mult * D[d][0]);
+                for (int d = 0; d < 3; ++d) x[d * kSub] += mult * D[d][0];
+                col += 3;
                 break;
             case CGX_VECTOR_GRADIENT_G2P:
-                if (NDOF >= 3) {
 #pragma unroll
-                    for (int a = 0; a < 3; ++a)
+                for (int a = 0; a < 3; ++a)
 #pragma unroll
-                        for (int b = 0; b < 3; ++b) add_field<float>(op.x, p, a * 3 + b, mult * D[a][b < NDOF ? b : 0]);
-                }
+                    for (int b = 0; b < 3; ++b) x[(a * 3 + b) * kSub] += mult * D[a][b < NDOF ? b : 0];
+                col += 9;
                 break;
             case CGX_VECTOR_DIVERGENCE_G2P:
-                if (NDOF >= 3) add_field<float>(op.x, p, 0, (D[0][0] + D[1][1 < NDOF ? 1 : 0] + D[2][2 < NDOF ? 2 : 0]) * mult);
+                x[0] += (D[0][0] + D[1][1 < NDOF ? 1 : 0] + D[2][2 < NDOF ? 2 : 0]) * mult;
+                col += 1;
                 break;
         }
     }
 }
 
 template <int ORDER, int NDOF, bool GRAD>
-__global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2)
+__global__ void __launch_bounds__(kThreads, 2)
     g2p_tiled_kernel(const __grid_constant__ TiledParams prm, int slot) {
     constexpr int K = ORDER + 1;
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) float smem[];
+    const TiledArray& ta = prm.arrays[slot];
+    const int box_floats = (prm.box_nodes * ta.a.dofs + 3) & ~3;
+    float* box = smem;
+    float4* prep = reinterpret_cast<float4*>(smem + box_floats);
+    float* out = reinterpret_cast<float*>(prep + kSub);
     __shared__ int item_idx;
     const int64_t nwork = *prm.work_count;
-    const TiledArray& ta = prm.arrays[slot];
     while (true) {
         if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
         __syncthreads();
@@ -168,60 +203,87 @@ __global__ void __launch_bounds__(kThreads, ORDER >= 3 ? 1 : 2)
                 float v = 0.0f;
                 if (gi < prm.mesh.ext[0] && gj < prm.mesh.ext[1] && gk < prm.mesh.ext[2])
                     v = load_array<float>(ta.a, node_index(prm.mesh, gi, gj, gk), dof);
-                smem[e] = v;
+                box[e] = v;
             }
         }
-        __syncthreads();
-
-        // Software pipeline: the next particle's coordinates are loaded and
-        // its output lines prefetched while the current one is computed.
-        double xn[3] = {0.0, 0.0, 0.0};
-        int64_t p = it.begin + threadIdx.x;
-        if (p < it.end) {
+        for (int64_t sb = it.begin; sb < it.end; sb += kSub) {
+            const int len = int((it.end - sb < kSub) ? it.end - sb : kSub);
+            // 1. load
+            for (int i = threadIdx.x; i < len; i += blockDim.x) {
+                const int64_t p = sb + i;
+                int s[3];
+                float u[3];
+                int key;
+                if (!form_point<ORDER>(prm, p, s, u)) {
+                    raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+                    key = kKeyInvalid;
+                } else {
+                    int l[3];
+                    bool inbox = true;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, p, d);
-        }
-        for (; p < it.end; p += blockDim.x) {
-            double x[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) x[d] = xn[d];
-            const int64_t pn = p + blockDim.x;
-            if (pn < it.end) {
-#pragma unroll
-                for (int d = 0; d < 3; ++d) xn[d] = load_field<double>(prm.points, pn, d);
+                    for (int d = 0; d < 3; ++d) {
+                        l[d] = s[d] - origin[d];
+                        inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
+                    }
+                    key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : kKeyOutside;
+                }
+                prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
+                int col = 0;
                 for (int o = 0; o < prm.n_ops; ++o) {
-                    if (prm.ops[o].slot != slot) continue;
-                    const int kind = prm.ops[o].kind;
-                    const int last = kind == CGX_VECTOR_GRADIENT_G2P ? 8
-                                     : (kind == CGX_VECTOR_VALUE_G2P || kind == CGX_SCALAR_GRADIENT_G2P) ? 2 : 0;
-                    prefetch_field(prm.ops[o].x, pn, 0);
-                    if (last) prefetch_field(prm.ops[o].x, pn, last);
+                    const DOp& op = prm.ops[o];
+                    if (op.slot != slot) continue;
+                    const int nc = dev_g2p_comps(op.kind);
+                    for (int c = 0; c < nc; ++c) out[(col + c) * kSub + i] = load_field<float>(op.x, p, c);
+                    col += nc;
                 }
             }
-            int s[3];
-            float u[3];
-            if (!form_point<ORDER>(prm, x, s, u)) {
-                raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
-                continue;
-            }
-            float w[3][K], g[3][K];
+            __syncthreads();
+            // 2. compute
+            for (int i = threadIdx.x; i < len; i += blockDim.x) {
+                const float4 pu = prep[i];
+                const int key = __float_as_int(pu.w);
+                if (key == kKeyInvalid) continue;
+                const float u[3] = {pu.x, pu.y, pu.z};
+                float w[3][K], g[3][K];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
-            int l[3];
-            bool inbox = true;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                l[d] = s[d] - origin[d];
-                inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
+                for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+                float V[NDOF], D[3][3];
+                int l[3], s[3];
+                if (key >= 0) {
+                    l[2] = key % prm.box[2];
+                    l[1] = (key / prm.box[2]) % prm.box[1];
+                    l[0] = key / (prm.box[1] * prm.box[2]);
+                    gather_sums<ORDER, NDOF, GRAD, true>(prm, ta, box, l, s, w, g, V, D);
+                } else {
+                    float uu[3];
+                    form_point<ORDER>(prm, sb + i, s, uu);
+                    gather_sums<ORDER, NDOF, GRAD, false>(prm, ta, box, l, s, w, g, V, D);
+                }
+                apply_ops<NDOF>(prm, slot, out, i, V, D);
             }
-            float V[NDOF], D[3][3];
-            if (inbox)
-                gather_sums<ORDER, NDOF, GRAD, true>(prm, ta, smem, l, s, w, g, V, D);
-            else
-                gather_sums<ORDER, NDOF, GRAD, false>(prm, ta, smem, l, s, w, g, V, D);
-            apply_ops<NDOF>(prm, slot, p, V, D);
+            __syncthreads();
+            // 3. store
+            for (int i = threadIdx.x; i < len; i += blockDim.x) {
+                const int64_t p = sb + i;
+                int col = 0;
+                for (int o = 0; o < prm.n_ops; ++o) {
+                    const DOp& op = prm.ops[o];
+                    if (op.slot != slot) continue;
+                    const int nc = dev_g2p_comps(op.kind);
+                    const int64_t base = field_base(op.x, p);
+                    for (int c = 0; c < nc; ++c) {
+                        const int64_t off = base + int64_t(c) * op.x.comp_stride;
+                        const float v = out[(col + c) * kSub + i];
+                        if (op.x.dtype == CGX_F64)
+                            reinterpret_cast<double*>(op.x.data)[off] = double(v);
+                        else
+                            reinterpret_cast<float*>(op.x.data)[off] = v;
+                    }
+                    col += nc;
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -264,6 +326,21 @@ void g2p_slot_need(const TiledParams& prm, int slot, int& ndof, bool& grad) {
             case CGX_VECTOR_DIVERGENCE_G2P: ndof = 3; grad = true; break;
         }
     }
+}
+
+size_t g2p_tiled_smem(const TiledParams& prm, int slot) {
+    int cols = 0;
+    bool f64_out = false;
+    for (int o = 0; o < prm.n_ops; ++o)
+        if (prm.ops[o].slot == slot) {
+            cols += g2p_comps(prm.ops[o].kind);
+            f64_out |= prm.ops[o].x.dtype == CGX_F64;
+        }
+    // Point fields are staged as FP32: double fields, or too many components,
+    // are left to the point-parallel kernel.
+    if (cols > kMaxOutCols || f64_out) return size_t(1) << 30;
+    const size_t box = size_t((prm.box_nodes * prm.arrays[slot].a.dofs + 3) & ~3) * sizeof(float);
+    return box + size_t(kSub) * sizeof(float4) + size_t(cols) * kSub * sizeof(float);
 }
 
 cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sms, size_t smem, cudaStream_t st) {
