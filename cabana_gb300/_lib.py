@@ -28,8 +28,12 @@ CGX_FLAG_SKIP_HALO = 1
 CGX_FLAG_CHECK_BOUNDS = 2
 
 # Every exported symbol declared in include/cgx.h.
+CGX_DISPATCH_NONE = 0
+CGX_DISPATCH_POINTS = 1
+CGX_DISPATCH_TILED = 2
+
 EXPORTS = (
-    "cgx_create", "cgx_destroy", "cgx_last_error", "cgx_version",
+    "cgx_create", "cgx_destroy", "cgx_last_error", "cgx_version", "cgx_last_dispatch",
     "cgx_p2g", "cgx_g2p", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
     "cgx_cartesian_num_bins", "cgx_linked_cell_build", "cgx_bin_by_key", "cgx_permute",
     "cgx_tiling_init", "cgx_tiling_num_offsets", "cgx_sort_tiles",
@@ -108,6 +112,8 @@ def lib():
     L.cgx_destroy.argtypes = [vp]
     L.cgx_last_error.restype = ctypes.c_char_p
     L.cgx_version.restype = ctypes.c_char_p
+    L.cgx_last_dispatch.argtypes = [vp]
+    L.cgx_last_dispatch.restype = ctypes.c_int
     interp = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, ctypes.c_int, P(CgxOp), ctypes.c_int, ctypes.c_int,
               P(CgxTiling), ctypes.c_uint, vp]
     L.cgx_p2g.argtypes = interp

@@ -18,6 +18,7 @@ struct cgx_context {
     size_t work_cap = 0;
     int64_t* work_prefix = nullptr;
     size_t prefix_cap = 0;
+    int last_dispatch = CGX_DISPATCH_NONE;
 };
 
 namespace {
@@ -348,8 +349,11 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
         if (s) return s;
     }
 
+    // The tiled kernels are built for cubic tiles of kTiledTile base nodes;
+    // other tilings still order the particles but run the point kernels.
     bool tiled = num_point > 0 && tiling && precision == CGX_FP32_COMPENSATED && tiling->tile_offsets &&
-                 tiling->spline_order == spline_order && spline_order >= 1 && spline_order <= 3;
+                 tiling->spline_order == spline_order && spline_order >= 1 && spline_order <= 3 &&
+                 tiling->tile[0] == kTiledTile && tiling->tile[1] == kTiledTile && tiling->tile[2] == kTiledTile;
     if (tiled) {
         TiledParams prm;
         std::memset(&prm, 0, sizeof(prm));
@@ -418,6 +422,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
                     CGX_CUDA(launch_g2p_tiled(one, spline_order, a, h->sms, smem_a, st));
                 }
             }
+            h->last_dispatch = CGX_DISPATCH_TILED;
         }
     }
     if (!tiled && num_point > 0) {
@@ -439,6 +444,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
             prm.ops[o].a.dofs = ops[o].array.dofs;
         }
         CGX_CUDA(launch_points(prm, spline_order, p2g, precision == CGX_PLAIN_FP64, h->sms, st));
+        h->last_dispatch = CGX_DISPATCH_POINTS;
     }
     if (p2g && !(flags & CGX_FLAG_SKIP_HALO)) {
         s = halo_all(*mesh, ops, n_ops, true, h->sms, st);
@@ -489,6 +495,8 @@ cgx_status cgx_destroy(cgx_handle h) {
 const char* cgx_last_error(void) { return g_last_error.c_str(); }
 
 const char* cgx_version(void) { return "cgx 0.1 (sm_103a)"; }
+
+int cgx_last_dispatch(cgx_handle h) { return h ? h->last_dispatch : CGX_DISPATCH_NONE; }
 
 cgx_status cgx_p2g(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point, int spline_order,
                    const cgx_op* ops, int n_ops, int precision, const cgx_tiling* tiling, unsigned flags,

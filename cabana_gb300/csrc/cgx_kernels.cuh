@@ -71,6 +71,10 @@ struct ChannelGroup {
     int8_t reserved;
 };
 
+// Cubic tile edge (base nodes) of the tiled kernels; the node box of a tile
+// is kTiledTile + order nodes per dimension, a compile-time constant.
+constexpr int kTiledTile = 8;
+
 constexpr int kMaxChannels = 24;
 constexpr int kMaxGroups = 16;
 

@@ -124,10 +124,11 @@ __device__ __forceinline__ float pick(const float* v, int idx) {
 // Direct (per-point) contribution of one group: compensated shared atomics
 // into the box, or global atomics when the stencil is outside the box. Each
 // lane walks its stencil starting at a different node.
-template <int ORDER, int CH, bool GRAD>
+template <int ORDER, int TILE, int CH, bool GRAD>
 __device__ __forceinline__ void add_direct(const TiledParams& prm, float* box_smem, const ChanSmem* cs, int first,
                                            int count, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
                                            const float (*coef)[3], bool inbox, const int* l, const int* s, int lane) {
+    constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
     constexpr int NODES = K * K * K;
     int node = lane % NODES;
@@ -144,7 +145,7 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, float* box_sm
         } else {
             wv = wi * wj * wk;
         }
-        const int bnode = inbox ? ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k) : 0;
+        const int bnode = inbox ? ((l[0] + i) * BB + (l[1] + j)) * BB + (l[2] + k) : 0;
         const int64_t gnode = inbox ? 0 : node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
@@ -212,16 +213,17 @@ __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 
 }
 
 // Reduce the warp's register sums and add them to the box.
-template <int ORDER, int CH, int NPAD>
+template <int ORDER, int TILE, int CH, int NPAD>
 __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const TiledParams& prm, float* box_smem,
                                           const ChanSmem* cs, int first, int count) {
+    constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
     constexpr int NODES = K * K * K;
     constexpr int R = NPAD / 32;
     transpose_reduce<NPAD>(acc, lane);
-    const int l2 = key % prm.box[2];
-    const int l1 = (key / prm.box[2]) % prm.box[1];
-    const int l0 = key / (prm.box[1] * prm.box[2]);
+    const int l2 = key % BB;
+    const int l1 = (key / BB) % BB;
+    const int l0 = key / (BB * BB);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int idx = lane * R + r;
@@ -229,7 +231,7 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
         const int c = idx - node * CH;
         if (node < NODES && c < count && acc[r] != 0.0f) {
             const int i = node / (K * K), j = (node / K) % K, k = node % K;
-            const int bnode = ((l0 + i) * prm.box[1] + (l1 + j)) * prm.box[2] + (l2 + k);
+            const int bnode = ((l0 + i) * BB + (l1 + j)) * BB + (l2 + k);
             const ChanSmem m = cs[first + c];
             const int e = m.sum_base + bnode * m.dofs;
             comp_add(box_smem + e, box_smem + e + m.comp_off, acc[r]);
@@ -242,10 +244,11 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
 // One warp processes item-local particles [b, e) for channel group gi.
 // prep[i] = (u0, u1, u2, key) of item particle i; srcs[s * kChunk + i] is
 // source s of item particle i (multiplier applied).
-template <int ORDER, bool GRAD>
+template <int ORDER, int TILE, bool GRAD>
 __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_smem, const float4* prep,
                                           const float* srcs, const ChanSmem* cs, int gi, const int* origin,
                                           int64_t item_begin, int b, int e, int lane) {
+    constexpr int BB = TILE + ORDER;  // node box extent per dimension
     using SH = P2GShape<ORDER>;
     constexpr int K = SH::K;
     constexpr int CH = GRAD ? SH::CG : SH::CV;
@@ -296,7 +299,7 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
                 rem &= rem - 1;
                 const int sk = __shfl_sync(0xffffffffu, key, sl);
                 if (sk != cur_key || run_windows == kMaxRunWindows) {
-                    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
+                    if (cur_key >= 0) flush_run<ORDER, TILE, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
                     cur_key = sk;
                     run_windows = 0;
                 }
@@ -305,7 +308,7 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
             }
         } else {
             if (cur_key >= 0) {
-                flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
+                flush_run<ORDER, TILE, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
                 cur_key = -1;
                 run_windows = 0;
             }
@@ -313,23 +316,24 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
                 int l[3], s[3];
                 bool inbox = key >= 0;
                 if (inbox) {
-                    l[2] = key % prm.box[2];
-                    l[1] = (key / prm.box[2]) % prm.box[1];
-                    l[0] = key / (prm.box[1] * prm.box[2]);
+                    l[2] = key % BB;
+                    l[1] = (key / BB) % BB;
+                    l[0] = key / (BB * BB);
                     for (int d = 0; d < 3; ++d) s[d] = origin[d] + l[d];
                 } else {
                     float uu[3];
                     form_point<ORDER>(prm, item_begin + i, s, uu);
                 }
-                add_direct<ORDER, CH, GRAD>(prm, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
+                add_direct<ORDER, TILE, CH, GRAD>(prm, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
             }
         }
     }
-    if (cur_key >= 0) flush_run<ORDER, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
+    if (cur_key >= 0) flush_run<ORDER, TILE, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
 }
 
-template <int ORDER>
+template <int ORDER, int TILE>
 __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_constant__ TiledParams prm) {
+    constexpr int BB = TILE + ORDER;  // node box extent per dimension
     using SH = P2GShape<ORDER>;
     constexpr int K = ORDER + 1;
     extern __shared__ __align__(16) float smem[];
@@ -344,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         const Channel ch = prm.channels[c];
         const TiledArray& ta = prm.arrays[ch.slot];
         cs[c].sum_base = ta.smem_offset + ch.dof;
-        cs[c].comp_off = prm.box_nodes * ta.a.dofs;
+        cs[c].comp_off = (BB * BB * BB) * ta.a.dofs;
         cs[c].dofs = ta.a.dofs;
     }
     const int ng = prm.n_groups;
@@ -404,9 +408,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     l[d] = s[d] - origin[d];
-                    inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
+                    inbox &= (l[d] >= 0) && (l[d] + K <= BB);
                 }
-                key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : kKeyOutside;
+                key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
             }
             prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
             for (int sidx = 0; sidx < prm.n_sources; ++sidx)
@@ -422,17 +426,17 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int e = (b + per < len) ? b + per : len;
                 if (b < e) {
                     if (prm.groups[gi].gradient)
-                        run_group<ORDER, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
+                        run_group<ORDER, TILE, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
                     else
-                        run_group<ORDER, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
+                        run_group<ORDER, TILE, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
                 }
             }
         } else {
             for (int gi = warp; gi < ng; gi += kWarps) {
                 if (prm.groups[gi].gradient)
-                    run_group<ORDER, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
+                    run_group<ORDER, TILE, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
                 else
-                    run_group<ORDER, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
+                    run_group<ORDER, TILE, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
             }
         }
         __syncthreads();
@@ -440,19 +444,21 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         for (int slot = 0; slot < prm.n_arrays; ++slot) {
             const TiledArray& ta = prm.arrays[slot];
             const int dofs = ta.a.dofs;
-            const int count = prm.box_nodes * dofs;
+            const int count = (BB * BB * BB) * dofs;
             const float* sum = box_smem + ta.smem_offset;
             const float* comp = sum + count;
-            for (int e = threadIdx.x; e < count; e += blockDim.x) {
-                const float v = sum[e] + comp[e];
-                if (v == 0.0f) continue;
-                const int node = e / dofs, dof = e - node * dofs;
-                const int bk = node % prm.box[2];
-                const int bj = (node / prm.box[2]) % prm.box[1];
-                const int bi = node / (prm.box[1] * prm.box[2]);
+            for (int node = threadIdx.x; node < BB * BB * BB; node += blockDim.x) {
+                const int bk = node % BB;
+                const int bj = (node / BB) % BB;
+                const int bi = node / (BB * BB);
                 const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
                 if (gi >= prm.mesh.ext[0] || gj >= prm.mesh.ext[1] || gk >= prm.mesh.ext[2]) continue;
-                atomic_add_array(ta.a, node_index(prm.mesh, gi, gj, gk), dof, v);
+                const int64_t gnode = node_index(prm.mesh, gi, gj, gk);
+                for (int dof = 0; dof < dofs; ++dof) {
+                    const int e = node * dofs + dof;
+                    const float v = sum[e] + comp[e];
+                    if (v != 0.0f) atomic_add_array(ta.a, gnode, dof, v);
+                }
             }
         }
         __syncthreads();
@@ -465,15 +471,16 @@ size_t smem_bytes(const TiledParams& prm, size_t box_bytes) {
 
 template <int ORDER>
 cudaError_t launch_order(const TiledParams& prm, int sms, size_t box_bytes, cudaStream_t st) {
+    constexpr int TILE = kTiledTile;
     const size_t smem = smem_bytes(prm, box_bytes);
-    const void* fn = reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER>);
+    const void* fn = reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER, TILE>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    p2g_tiled_kernel<ORDER><<<sms * per_sm, kThreads, smem, st>>>(prm);
+    p2g_tiled_kernel<ORDER, TILE><<<sms * per_sm, kThreads, smem, st>>>(prm);
     return cudaGetLastError();
 }
 

@@ -61,10 +61,11 @@ __device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, in
 }
 
 // Gather sums for one array: V[n] = sum W v_n, D[m][n] = sum d_m W v_n.
-template <int ORDER, int NDOF, bool GRAD, bool BOXED>
+template <int ORDER, int TILE, int NDOF, bool GRAD, bool BOXED>
 __device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledArray& ta, const float* box,
                                             const int* l, const int* s, const float (*w)[ORDER + 1],
                                             const float (*g)[ORDER + 1], float* V, float (*D)[3]) {
+    constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
     const int dofs = ta.a.dofs;
 #pragma unroll
@@ -87,7 +88,7 @@ __device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledA
             for (int k = 0; k < K; ++k) {
                 float v[NDOF];
                 if (BOXED) {
-                    const int node = ((l[0] + i) * prm.box[1] + (l[1] + j)) * prm.box[2] + (l[2] + k);
+                    const int node = ((l[0] + i) * BB + (l[1] + j)) * BB + (l[2] + k);
 #pragma unroll
                     for (int n = 0; n < NDOF; ++n) v[n] = box[node * dofs + n];
                 } else {
@@ -163,13 +164,14 @@ __device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, floa
     }
 }
 
-template <int ORDER, int NDOF, bool GRAD>
+template <int ORDER, int TILE, int NDOF, bool GRAD>
 __global__ void __launch_bounds__(kThreads, 2)
     g2p_tiled_kernel(const __grid_constant__ TiledParams prm, int slot) {
+    constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
     extern __shared__ __align__(16) float smem[];
     const TiledArray& ta = prm.arrays[slot];
-    const int box_floats = (prm.box_nodes * ta.a.dofs + 3) & ~3;
+    const int box_floats = ((BB * BB * BB) * ta.a.dofs + 3) & ~3;
     float* box = smem;
     float4* prep = reinterpret_cast<float4*>(smem + box_floats);
     float* out = reinterpret_cast<float*>(prep + kSub);
@@ -193,17 +195,14 @@ __global__ void __launch_bounds__(kThreads, 2)
         // Stage the node box of the source array (coalesced rows of k * dofs).
         {
             const int dofs = ta.a.dofs;
-            const int row = prm.box[2] * dofs;
-            const int count = prm.box_nodes * dofs;
-            for (int e = threadIdx.x; e < count; e += blockDim.x) {
-                const int r = e / row, c = e - r * row;
-                const int bj = r % prm.box[1], bi = r / prm.box[1];
-                const int bk = c / dofs, dof = c - bk * dofs;
+            for (int node = threadIdx.x; node < BB * BB * BB; node += blockDim.x) {
+                const int bk = node % BB;
+                const int bj = (node / BB) % BB;
+                const int bi = node / (BB * BB);
                 const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
-                float v = 0.0f;
-                if (gi < prm.mesh.ext[0] && gj < prm.mesh.ext[1] && gk < prm.mesh.ext[2])
-                    v = load_array<float>(ta.a, node_index(prm.mesh, gi, gj, gk), dof);
-                box[e] = v;
+                const bool in = gi < prm.mesh.ext[0] && gj < prm.mesh.ext[1] && gk < prm.mesh.ext[2];
+                const int64_t gnode = in ? node_index(prm.mesh, gi, gj, gk) : 0;
+                for (int dof = 0; dof < dofs; ++dof) box[node * dofs + dof] = in ? load_array<float>(ta.a, gnode, dof) : 0.0f;
             }
         }
         for (int64_t sb = it.begin; sb < it.end; sb += kSub) {
@@ -223,9 +222,9 @@ __global__ void __launch_bounds__(kThreads, 2)
 #pragma unroll
                     for (int d = 0; d < 3; ++d) {
                         l[d] = s[d] - origin[d];
-                        inbox &= (l[d] >= 0) && (l[d] + K <= prm.box[d]);
+                        inbox &= (l[d] >= 0) && (l[d] + K <= BB);
                     }
-                    key = inbox ? (l[0] * prm.box[1] + l[1]) * prm.box[2] + l[2] : kKeyOutside;
+                    key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
                 }
                 prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
                 int col = 0;
@@ -250,14 +249,14 @@ __global__ void __launch_bounds__(kThreads, 2)
                 float V[NDOF], D[3][3];
                 int l[3], s[3];
                 if (key >= 0) {
-                    l[2] = key % prm.box[2];
-                    l[1] = (key / prm.box[2]) % prm.box[1];
-                    l[0] = key / (prm.box[1] * prm.box[2]);
-                    gather_sums<ORDER, NDOF, GRAD, true>(prm, ta, box, l, s, w, g, V, D);
+                    l[2] = key % BB;
+                    l[1] = (key / BB) % BB;
+                    l[0] = key / (BB * BB);
+                    gather_sums<ORDER, TILE, NDOF, GRAD, true>(prm, ta, box, l, s, w, g, V, D);
                 } else {
                     float uu[3];
                     form_point<ORDER>(prm, sb + i, s, uu);
-                    gather_sums<ORDER, NDOF, GRAD, false>(prm, ta, box, l, s, w, g, V, D);
+                    gather_sums<ORDER, TILE, NDOF, GRAD, false>(prm, ta, box, l, s, w, g, V, D);
                 }
                 apply_ops<NDOF>(prm, slot, out, i, V, D);
             }
@@ -289,14 +288,14 @@ __global__ void __launch_bounds__(kThreads, 2)
 
 template <int ORDER, int NDOF, bool GRAD>
 cudaError_t launch_g2p(const TiledParams& prm, int slot, int sms, size_t smem, cudaStream_t st) {
-    const void* fn = reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER, NDOF, GRAD>);
+    const void* fn = reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER, kTiledTile, NDOF, GRAD>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    g2p_tiled_kernel<ORDER, NDOF, GRAD><<<sms * per_sm, kThreads, smem, st>>>(prm, slot);
+    g2p_tiled_kernel<ORDER, kTiledTile, NDOF, GRAD><<<sms * per_sm, kThreads, smem, st>>>(prm, slot);
     return cudaGetLastError();
 }
 

@@ -306,6 +306,13 @@ def g2p(array, halo: Optional[Halo], points, num_point, spline: Spline, functor,
                             len(fs), precision, til, fl, _stream(stream)))
 
 
+def last_dispatch(handle=None):
+    """Kernel family of the last p2g / g2p on the handle: 'points' or 'tiled'."""
+    h = handle or L.default_handle()
+    return {L.CGX_DISPATCH_NONE: None, L.CGX_DISPATCH_POINTS: "points",
+            L.CGX_DISPATCH_TILED: "tiled"}[L.lib().cgx_last_dispatch(h.ptr)]
+
+
 class Tiling:
     """Tile-major ordering of particles for the tiled kernels."""
 

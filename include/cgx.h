@@ -150,6 +150,14 @@ cgx_status cgx_destroy(cgx_handle h);
 const char* cgx_last_error(void);
 const char* cgx_version(void);
 
+/* Kernel family used by the last cgx_p2g / cgx_g2p on this handle (no
+ * reference counterpart; for tests and tuning). The tiled family needs
+ * CGX_FP32_COMPENSATED, spline order 1-3 and a tiling with tile 8x8x8. */
+#define CGX_DISPATCH_NONE 0
+#define CGX_DISPATCH_POINTS 1
+#define CGX_DISPATCH_TILED 2
+int cgx_last_dispatch(cgx_handle h);
+
 /* ---- interpolation ---------------------------------------------------- */
 
 /*

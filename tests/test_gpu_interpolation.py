@@ -43,7 +43,7 @@ def sorted_inputs(mp, order, pts, fields, tiled):
     tf = [torch.tensor(f, device="cuda") for f in fields]
     if not tiled:
         return tp, tf, None, None
-    til = G.Tiling(mp, order, (4, 4, 4))
+    til = G.Tiling(mp, order, (8, 8, 8))
     perm = til.sort(tp, tp.shape[0])
     from cabana_gb300 import core
     core.permute_by(perm, tp, *tf)
@@ -113,6 +113,7 @@ def _p2g_case(oracle, order, kind, precision, tiled, seed, clumped=False, n=3000
           G.createTensorDivergenceP2G][kind]
     G.p2g(mk(tx, 0.75), tp, n, G.Spline(order), G.createHalo(G.NodeHaloPattern(), mp.halo_width), arr,
           precision=precision, tiling=til, check_bounds=True)
+    assert G.last_dispatch() == ("tiled" if tiled and order in (1, 2, 3) else "points")
     return arr.view().double().cpu().numpy(), ref
 
 
@@ -147,6 +148,7 @@ def _g2p_case(oracle, order, kind, precision, tiled, seed, n=3000, entity=M.NODE
           G.createVectorDivergenceG2P][kind]
     G.g2p(arr, G.createHalo(G.NodeHaloPattern(), mp.halo_width), tp, n, G.Spline(order), mk(tx, -1.25),
           precision=precision, tiling=til, check_bounds=True)
+    assert G.last_dispatch() == ("tiled" if tiled and order in (1, 2, 3) else "points")
     got = tx.double().cpu().numpy().reshape(n, -1)
     if perm is not None:
         ref = ref[perm]
