@@ -413,8 +413,20 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
             }
             prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
-            for (int sidx = 0; sidx < prm.n_sources; ++sidx)
-                srcs[sidx * kChunk + i] = load_src(prm, prm.sources[sidx], it.begin + i);
+        }
+        // Sources, one at a time: coalesced loads of one component.
+        for (int sidx = 0; sidx < prm.n_sources; ++sidx) {
+            const Source src = prm.sources[sidx];
+            const DField f = prm.ops[src.op].x;
+            float* dst = srcs + sidx * kChunk;
+            if (f.log2vl == 0 && f.dtype == CGX_F32) {
+                const float* base = reinterpret_cast<const float*>(f.data) + int64_t(src.comp) * f.comp_stride +
+                                    it.begin * f.soa_stride;
+                const int64_t stride = f.soa_stride;
+                for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = __ldg(base + i * stride) * src.mult;
+            } else {
+                for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(prm, src, it.begin + i);
+            }
         }
         __syncthreads();
         if (ng <= kWarps) {

@@ -227,13 +227,26 @@ __global__ void __launch_bounds__(kThreads, 2)
                     key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
                 }
                 prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
+            }
+            // Current point-field values, one component at a time (the tiled
+            // path only takes FP32 point fields).
+            {
                 int col = 0;
                 for (int o = 0; o < prm.n_ops; ++o) {
                     const DOp& op = prm.ops[o];
                     if (op.slot != slot) continue;
                     const int nc = dev_g2p_comps(op.kind);
-                    for (int c = 0; c < nc; ++c) out[(col + c) * kSub + i] = load_field<float>(op.x, p, c);
-                    col += nc;
+                    for (int c = 0; c < nc; ++c, ++col) {
+                        float* dst = out + col * kSub;
+                        if (op.x.log2vl == 0) {
+                            const float* src = reinterpret_cast<const float*>(op.x.data) + int64_t(c) * op.x.comp_stride +
+                                               sb * op.x.soa_stride;
+                            const int64_t stride = op.x.soa_stride;
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i * stride];
+                        } else {
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_field<float>(op.x, sb + i, c);
+                        }
+                    }
                 }
             }
             __syncthreads();
@@ -262,23 +275,24 @@ __global__ void __launch_bounds__(kThreads, 2)
             }
             __syncthreads();
             // 3. store
-            for (int i = threadIdx.x; i < len; i += blockDim.x) {
-                const int64_t p = sb + i;
+            {
                 int col = 0;
                 for (int o = 0; o < prm.n_ops; ++o) {
                     const DOp& op = prm.ops[o];
                     if (op.slot != slot) continue;
                     const int nc = dev_g2p_comps(op.kind);
-                    const int64_t base = field_base(op.x, p);
-                    for (int c = 0; c < nc; ++c) {
-                        const int64_t off = base + int64_t(c) * op.x.comp_stride;
-                        const float v = out[(col + c) * kSub + i];
-                        if (op.x.dtype == CGX_F64)
-                            reinterpret_cast<double*>(op.x.data)[off] = double(v);
-                        else
-                            reinterpret_cast<float*>(op.x.data)[off] = v;
+                    for (int c = 0; c < nc; ++c, ++col) {
+                        const float* srcv = out + col * kSub;
+                        if (op.x.log2vl == 0) {
+                            float* dst = reinterpret_cast<float*>(op.x.data) + int64_t(c) * op.x.comp_stride +
+                                         sb * op.x.soa_stride;
+                            const int64_t stride = op.x.soa_stride;
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i * stride] = srcv[i];
+                        } else {
+                            float* data = reinterpret_cast<float*>(op.x.data);
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) data[field_offset(op.x, sb + i, c)] = srcv[i];
+                        }
                     }
-                    col += nc;
                 }
             }
             __syncthreads();
