@@ -70,6 +70,17 @@ __device__ __forceinline__ T load_field(const DField& f, int64_t p, int c) {
     return T(__ldg(reinterpret_cast<const float*>(f.data) + o));
 }
 
+// Asynchronous 4-byte global -> shared copy (no register round trip); all
+// copies issued by a thread complete at cp_async_wait_all().
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Ask the L1 to fetch the line holding element (p, c) of a field.
 __device__ __forceinline__ void prefetch_field(const DField& f, int64_t p, int c) {
     const int64_t o = field_offset(f, p, c) * (f.dtype == CGX_F64 ? 8 : 4);
@@ -219,17 +230,20 @@ __device__ __forceinline__ void base_and_offset(double x0, int& base, T& u) {
 // fraction bits, then to FP32 toward zero, so it is always < 1. Returns
 // false for t < 0, t >= 2^30 or NaN.
 __device__ __forceinline__ bool split_logical(double t, int& cell, float& u) {
-    if (!(t >= 0.0) || !(t < 1073741824.0)) {
-        cell = 0;
-        u = 0.0f;
-        return false;
-    }
+    // Range checks on the bits (no double-precision compares): negative,
+    // >= 2^30, infinite and NaN values all fail.
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(t));
-    const int e = int(b >> 52);
-    if (e == 0) {  // zero or subnormal
+    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+    const int e = int(mag >> 52);
+    if (mag == 0 || e == 0) {  // +-0 or subnormal
         cell = 0;
         u = 0.0f;
         return true;
+    }
+    if ((b >> 63) != 0 || e >= 1023 + 30) {
+        cell = 0;
+        u = 0.0f;
+        return false;
     }
     const unsigned long long sig = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const int sh = 1075 - e;  // t = sig * 2^-sh

@@ -92,6 +92,20 @@ struct ChanSmem {
 };
 
 template <int ORDER>
+__device__ __forceinline__ bool form_from(const TiledParams& prm, const double* x, int* s, float* u) {
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        int c;
+        ok &= split_logical(t, c, u[d]);
+        s[d] = c + first_offset(ORDER);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
+    }
+    return ok;
+}
+
+template <int ORDER>
 __device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, int* s, float* u) {
     bool ok = true;
 #pragma unroll
@@ -108,9 +122,9 @@ __device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, in
 __device__ __forceinline__ float load_src(const TiledParams& prm, const Source& src, int64_t p) {
     const DField& f = prm.ops[src.op].x;
     const int64_t o = field_base(f, p) + int64_t(src.comp) * f.comp_stride;
-    const float v = f.dtype == CGX_F64 ? float(__ldg(reinterpret_cast<const double*>(f.data) + o))
-                                       : __ldg(reinterpret_cast<const float*>(f.data) + o);
-    return v * src.mult;
+    // raw value: the multiplier is applied where the value is used
+    return f.dtype == CGX_F64 ? float(__ldg(reinterpret_cast<const double*>(f.data) + o))
+                              : __ldg(reinterpret_cast<const float*>(f.data) + o);
 }
 
 template <int K>
@@ -152,9 +166,12 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, float* box_sm
             if (c >= count) break;
             const float v = GRAD ? coef[c][0] * g0 + coef[c][1] * g1 + coef[c][2] * g2 : coef[c][0] * wv;
             if (inbox) {
+                // Single-particle terms go to the compensation half with a
+                // plain (non-returning) atomic: they are small next to the
+                // run sums held in the sum half, and the flush adds both.
                 const ChanSmem m = cs[first + c];
                 const int e = m.sum_base + bnode * m.dofs;
-                comp_add(box_smem + e, box_smem + e + m.comp_off, v);
+                atomicAdd(box_smem + e + m.comp_off, v);
             } else {
                 const Channel& ch = prm.channels[first + c];
                 atomic_add_array(prm.arrays[ch.slot].a, gnode, ch.dof, v);
@@ -258,10 +275,14 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
     const int first = grp.first, count = grp.count;
     // Shared-memory rows of this group's sources (-1: zero).
     int srow[CH][NS];
+    float smul[CH][NS];
 #pragma unroll
     for (int c = 0; c < CH; ++c)
 #pragma unroll
-        for (int n = 0; n < NS; ++n) srow[c][n] = c < count ? prm.channels[first + c].src[n] : -1;
+        for (int n = 0; n < NS; ++n) {
+            srow[c][n] = c < count ? prm.channels[first + c].src[n] : -1;
+            smul[c][n] = srow[c][n] >= 0 ? prm.sources[srow[c][n]].mult : 0.0f;
+        }
 
     float acc[NPAD];
 #pragma unroll
@@ -278,7 +299,7 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
                 const int r = n < NS ? srow[c][n < NS ? n : 0] : -1;
-                coef[c][n] = (r >= 0 && active) ? srcs[r * kChunk + i] : 0.0f;
+                coef[c][n] = (r >= 0 && active) ? srcs[r * kChunk + i] * smul[c][n < NS ? n : 0] : 0.0f;
             }
         float4 pu = active ? prep[i] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kKeyInvalid));
         const int key = __float_as_int(pu.w);
@@ -394,27 +415,8 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             origin[1] = t1 * prm.tile[1];
             origin[2] = t2 * prm.tile[2];
         }
-        // Prep: base node key in the box and in-cell offsets, once per particle.
-        for (int i = threadIdx.x; i < len; i += blockDim.x) {
-            int s[3];
-            float u[3];
-            int key;
-            if (!form_point<ORDER>(prm, it.begin + i, s, u)) {
-                raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
-                key = kKeyInvalid;
-            } else {
-                int l[3];
-                bool inbox = true;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    l[d] = s[d] - origin[d];
-                    inbox &= (l[d] >= 0) && (l[d] + K <= BB);
-                }
-                key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
-            }
-            prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
-        }
-        // Sources, one at a time: coalesced loads of one component.
+        // Sources (raw values; multipliers are applied at use): asynchronous
+        // copies, one component at a time, all in flight together.
         for (int sidx = 0; sidx < prm.n_sources; ++sidx) {
             const Source src = prm.sources[sidx];
             const DField f = prm.ops[src.op].x;
@@ -423,11 +425,47 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const float* base = reinterpret_cast<const float*>(f.data) + int64_t(src.comp) * f.comp_stride +
                                     it.begin * f.soa_stride;
                 const int64_t stride = f.soa_stride;
-                for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = __ldg(base + i * stride) * src.mult;
+                for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, base + i * stride);
             } else {
                 for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(prm, src, it.begin + i);
             }
         }
+        // Prep: base node key in the box and in-cell offsets, once per
+        // particle; the coordinates of all of a thread's particles are loaded
+        // before any is used.
+        {
+            constexpr int PER = kChunk / kThreads;
+            double xs[PER][3];
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int i = threadIdx.x + q * kThreads;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(prm.points, it.begin + i, d) : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int i = threadIdx.x + q * kThreads;
+                if (i >= len) continue;
+                int s[3];
+                float u[3];
+                int key;
+                if (!form_from<ORDER>(prm, xs[q], s, u)) {
+                    raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+                    key = kKeyInvalid;
+                } else {
+                    int l[3];
+                    bool inbox = true;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        l[d] = s[d] - origin[d];
+                        inbox &= (l[d] >= 0) && (l[d] + K <= BB);
+                    }
+                    key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
+                }
+                prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
+            }
+        }
+        cp_async_wait_all();
         __syncthreads();
         if (ng <= kWarps) {
             const int gi = warp_group[warp];

@@ -47,6 +47,20 @@ __device__ __forceinline__ int dev_g2p_comps(int kind) {
 }
 
 template <int ORDER>
+__device__ __forceinline__ bool form_from(const TiledParams& prm, const double* x, int* s, float* u) {
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        int c;
+        ok &= split_logical(t, c, u[d]);
+        s[d] = c + first_offset(ORDER);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
+    }
+    return ok;
+}
+
+template <int ORDER>
 __device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, int* s, float* u) {
     bool ok = true;
 #pragma unroll
@@ -207,29 +221,10 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
         for (int64_t sb = it.begin; sb < it.end; sb += kSub) {
             const int len = int((it.end - sb < kSub) ? it.end - sb : kSub);
-            // 1. load
-            for (int i = threadIdx.x; i < len; i += blockDim.x) {
-                const int64_t p = sb + i;
-                int s[3];
-                float u[3];
-                int key;
-                if (!form_point<ORDER>(prm, p, s, u)) {
-                    raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
-                    key = kKeyInvalid;
-                } else {
-                    int l[3];
-                    bool inbox = true;
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        l[d] = s[d] - origin[d];
-                        inbox &= (l[d] >= 0) && (l[d] + K <= BB);
-                    }
-                    key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
-                }
-                prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
-            }
-            // Current point-field values, one component at a time (the tiled
-            // path only takes FP32 point fields).
+            // 1. load. Current point-field values first, as asynchronous
+            // copies, one component at a time (the tiled path only takes FP32
+            // point fields); then the coordinates, all of a thread's particles
+            // loaded before any is used.
             {
                 int col = 0;
                 for (int o = 0; o < prm.n_ops; ++o) {
@@ -242,13 +237,46 @@ __global__ void __launch_bounds__(kThreads, 2)
                             const float* src = reinterpret_cast<const float*>(op.x.data) + int64_t(c) * op.x.comp_stride +
                                                sb * op.x.soa_stride;
                             const int64_t stride = op.x.soa_stride;
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i * stride];
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, src + i * stride);
                         } else {
                             for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_field<float>(op.x, sb + i, c);
                         }
                     }
                 }
             }
+            {
+                constexpr int PER = kSub / kThreads;
+                double xs[PER][3];
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const int i = threadIdx.x + q * kThreads;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(prm.points, sb + i, d) : 0.0;
+                }
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const int i = threadIdx.x + q * kThreads;
+                    if (i >= len) continue;
+                    int s[3];
+                    float u[3];
+                    int key;
+                    if (!form_from<ORDER>(prm, xs[q], s, u)) {
+                        raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+                        key = kKeyInvalid;
+                    } else {
+                        int l[3];
+                        bool inbox = true;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            l[d] = s[d] - origin[d];
+                            inbox &= (l[d] >= 0) && (l[d] + K <= BB);
+                        }
+                        key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
+                    }
+                    prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
+                }
+            }
+            cp_async_wait_all();
             __syncthreads();
             // 2. compute
             for (int i = threadIdx.x; i < len; i += blockDim.x) {
