@@ -397,7 +397,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
         const size_t smem = size_t(offset) * sizeof(float);
         // node boxes plus per-item staging must fit in one SM's shared memory
         if (p2g) {
-            if (p2g_tiled_smem(prm, smem) > 220 * 1024) tiled = false;
+            if (p2g_tiled_smem(prm, smem) > 210 * 1024) tiled = false;  // + ~9 KB static run table
         } else {
             for (int a = 0; a < n_arrays; ++a)
                 if (g2p_tiled_smem(prm, a) > 220 * 1024) tiled = false;

@@ -40,6 +40,7 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 2048;        // particles per work item (host builds items of this size)
 constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
+constexpr int kSmallRun = 12;       // shorter runs add each particle directly
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
 
@@ -258,22 +259,23 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
 }
 
-// One warp processes item-local particles [b, e) for channel group gi.
-// prep[i] = (u0, u1, u2, key) of item particle i; srcs[s * kChunk + i] is
-// source s of item particle i (multiplier applied).
+// One warp of channel group gi pulls cell runs of the current item from the
+// group's shared counter until none are left. prep[i] = (u0, u1, u2, key) of
+// item particle i; srcs[s * kChunk + i] is raw source s of item particle i;
+// runs[r] is the first particle of run r (runs[n_runs] = item length).
 template <int ORDER, int TILE, bool GRAD>
-__device__ __forceinline__ void run_group(const TiledParams& prm, float* box_smem, const float4* prep,
-                                          const float* srcs, const ChanSmem* cs, int gi, const int* origin,
-                                          int64_t item_begin, int b, int e, int lane) {
-    constexpr int BB = TILE + ORDER;  // node box extent per dimension
+__device__ __forceinline__ void process_runs(const TiledParams& prm, float* box_smem, const float4* prep,
+                                             const float* srcs, const int* runs, int n_runs, int* next_run,
+                                             const ChanSmem* cs, int gi, const int* origin, int64_t item_begin,
+                                             int lane) {
     using SH = P2GShape<ORDER>;
+    constexpr int BB = TILE + ORDER;
     constexpr int K = SH::K;
     constexpr int CH = GRAD ? SH::CG : SH::CV;
     constexpr int NPAD = GRAD ? SH::NG : SH::NV;
     constexpr int NS = GRAD ? 3 : 1;  // sources per channel
     const ChannelGroup grp = prm.groups[gi];
     const int first = grp.first, count = grp.count;
-    // Shared-memory rows of this group's sources (-1: zero).
     int srow[CH][NS];
     float smul[CH][NS];
 #pragma unroll
@@ -287,59 +289,48 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
     float acc[NPAD];
 #pragma unroll
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
-    int cur_key = -1;
-    int run_windows = 0;
 
-    for (int w0 = b; w0 < e; w0 += 32) {
-        const int i = w0 + lane;
-        const bool active = i < e;
-        float coef[CH][3];
+    while (true) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(next_run, 1);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r >= n_runs) break;
+        const int rb = runs[r], re = runs[r + 1];
+        const int key = __float_as_int(prep[rb].w);
+        if (key == kKeyInvalid) continue;
+        const bool big = key >= 0 && re - rb >= kSmallRun;
+        int windows = 0;
+        for (int w0 = rb; w0 < re; w0 += 32) {
+            const int i = w0 + lane;
+            const bool active = i < re;
+            float coef[CH][3];
 #pragma unroll
-        for (int c = 0; c < CH; ++c)
+            for (int c = 0; c < CH; ++c)
 #pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                const int r = n < NS ? srow[c][n < NS ? n : 0] : -1;
-                coef[c][n] = (r >= 0 && active) ? srcs[r * kChunk + i] * smul[c][n < NS ? n : 0] : 0.0f;
-            }
-        float4 pu = active ? prep[i] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kKeyInvalid));
-        const int key = __float_as_int(pu.w);
-        const float u[3] = {pu.x, pu.y, pu.z};
-        float w[3][K], g[3][K];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
-
-        // Sorted particles: lanes with one key are contiguous.
-        const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-        const unsigned starts = __ballot_sync(0xffffffffu, active && (lane == 0 || key != prev));
-        const bool all_in = __all_sync(0xffffffffu, !active || key >= 0);
-
-        if (all_in && __popc(starts) <= 2) {
-            unsigned rem = starts;
-            while (rem) {
-                const int sl = __ffs(rem) - 1;
-                rem &= rem - 1;
-                const int sk = __shfl_sync(0xffffffffu, key, sl);
-                if (sk != cur_key || run_windows == kMaxRunWindows) {
-                    if (cur_key >= 0) flush_run<ORDER, TILE, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
-                    cur_key = sk;
-                    run_windows = 0;
+                for (int n = 0; n < 3; ++n) {
+                    const int rr = n < NS ? srow[c][n < NS ? n : 0] : -1;
+                    coef[c][n] = (rr >= 0 && active) ? srcs[rr * kChunk + i] * smul[c][n < NS ? n : 0] : 0.0f;
                 }
-                ++run_windows;
-                accumulate<ORDER, CH, GRAD>(acc, w, g, coef, active && key == sk);
-            }
-        } else {
-            if (cur_key >= 0) {
-                flush_run<ORDER, TILE, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
-                cur_key = -1;
-                run_windows = 0;
-            }
-            if (active && key != kKeyInvalid) {
+            const float4 pu = active ? prep[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const float u[3] = {pu.x, pu.y, pu.z};
+            float w[3][K], g[3][K];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+            if (big) {
+                if (windows == kMaxRunWindows) {
+                    flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
+                    windows = 0;
+                }
+                ++windows;
+                accumulate<ORDER, CH, GRAD>(acc, w, g, coef, active);
+            } else if (active) {
                 int l[3], s[3];
-                bool inbox = key >= 0;
+                const bool inbox = key >= 0;
                 if (inbox) {
                     l[2] = key % BB;
                     l[1] = (key / BB) % BB;
                     l[0] = key / (BB * BB);
+#pragma unroll
                     for (int d = 0; d < 3; ++d) s[d] = origin[d] + l[d];
                 } else {
                     float uu[3];
@@ -348,8 +339,8 @@ __device__ __forceinline__ void run_group(const TiledParams& prm, float* box_sme
                 add_direct<ORDER, TILE, CH, GRAD>(prm, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
             }
         }
+        if (big) flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
     }
-    if (cur_key >= 0) flush_run<ORDER, TILE, CH, NPAD>(acc, lane, cur_key, prm, box_smem, cs, first, count);
 }
 
 template <int ORDER, int TILE>
@@ -363,7 +354,11 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     float* srcs = reinterpret_cast<float*>(prep + kChunk);
     __shared__ ChanSmem cs[kMaxChannels];
     __shared__ int item_idx;
-    __shared__ int warp_group[kWarps], warp_rank[kWarps], group_warps[kMaxGroups];
+    __shared__ int runs[kChunk + 1];
+    __shared__ int n_runs;
+    __shared__ int next_run[kMaxGroups];
+    __shared__ int warp_sums[kWarps];
+    __shared__ int warp_group[kWarps], group_warps[kMaxGroups];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int c = threadIdx.x; c < prm.n_channels; c += blockDim.x) {
         const Channel ch = prm.channels[c];
@@ -376,10 +371,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     if (threadIdx.x == 0) {
         // Share the warps among the groups in proportion to their arithmetic
         // (a gradient channel costs about twice a value channel).
-        int cost[kMaxGroups], total = 0;
+        int cost[kMaxGroups];
         for (int gi = 0; gi < ng; ++gi) {
             cost[gi] = prm.groups[gi].count * (prm.groups[gi].gradient ? 2 * SH::CV / SH::CG : 1);
-            total += cost[gi];
             group_warps[gi] = 1;
         }
         for (int left = kWarps - ng; left > 0 && ng > 0; --left) {
@@ -388,19 +382,21 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 if (cost[gi] * group_warps[best] > cost[best] * group_warps[gi]) best = gi;
             group_warps[best] += 1;
         }
-        (void)total;
         int w = 0;
         for (int gi = 0; gi < ng && w < kWarps; ++gi)
-            for (int r = 0; r < group_warps[gi] && w < kWarps; ++r, ++w) {
-                warp_group[w] = gi;
-                warp_rank[w] = r;
-            }
+            for (int r = 0; r < group_warps[gi] && w < kWarps; ++r, ++w) warp_group[w] = gi;
         for (; w < kWarps; ++w) warp_group[w] = -1;
     }
     const int64_t nwork = *prm.work_count;
     while (true) {
         if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
-        for (int i = threadIdx.x; i < prm.smem_floats; i += blockDim.x) box_smem[i] = 0.0f;
+        if (threadIdx.x < kMaxGroups) next_run[threadIdx.x] = 0;
+        for (int i = threadIdx.x * 4; i < prm.smem_floats; i += blockDim.x * 4) {
+            if (i + 3 < prm.smem_floats)
+                *reinterpret_cast<float4*>(box_smem + i) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            else
+                for (int j = i; j < prm.smem_floats; ++j) box_smem[j] = 0.0f;
+        }
         __syncthreads();
         const int64_t widx = item_idx;
         if (widx >= nwork) break;
@@ -430,28 +426,28 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(prm, src, it.begin + i);
             }
         }
-        // Prep: base node key in the box and in-cell offsets, once per
-        // particle; the coordinates of all of a thread's particles are loaded
-        // before any is used.
+        // Prep: base node key in the box and in-cell offsets of each thread's
+        // kChunk / kThreads consecutive particles (coordinates all loaded
+        // before any is used), then the runs of equal keys.
+        constexpr int PER = kChunk / kThreads;
+        int keys[PER];
         {
-            constexpr int PER = kChunk / kThreads;
             double xs[PER][3];
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x + q * kThreads;
+                const int i = threadIdx.x * PER + q;
 #pragma unroll
                 for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(prm.points, it.begin + i, d) : 0.0;
             }
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x + q * kThreads;
+                const int i = threadIdx.x * PER + q;
+                keys[q] = kKeyInvalid;
                 if (i >= len) continue;
                 int s[3];
                 float u[3];
-                int key;
                 if (!form_from<ORDER>(prm, xs[q], s, u)) {
                     raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
-                    key = kKeyInvalid;
                 } else {
                     int l[3];
                     bool inbox = true;
@@ -460,33 +456,67 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                         l[d] = s[d] - origin[d];
                         inbox &= (l[d] >= 0) && (l[d] + K <= BB);
                     }
-                    key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
+                    keys[q] = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
                 }
-                prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
+                prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(keys[q]));
             }
         }
         cp_async_wait_all();
         __syncthreads();
-        if (ng <= kWarps) {
-            const int gi = warp_group[warp];
-            if (gi >= 0) {
-                const int wpg = group_warps[gi], r = warp_rank[warp];
-                const int per = ((len + wpg - 1) / wpg + 31) / 32 * 32;
-                const int b = r * per;
-                const int e = (b + per < len) ? b + per : len;
-                if (b < e) {
-                    if (prm.groups[gi].gradient)
-                        run_group<ORDER, TILE, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
-                    else
-                        run_group<ORDER, TILE, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, b, e, lane);
-                }
+        // Run starts: particle i starts a run when its key differs from i-1.
+        {
+            int flags = 0, nstart = 0;
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int i = threadIdx.x * PER + q;
+                int prev = kKeyInvalid - 1;
+                if (i > 0) prev = q == 0 ? __float_as_int(prep[i - 1].w) : keys[q - 1];
+                const bool st = i < len && keys[q] != prev;
+                flags |= st ? (1 << q) : 0;
+                nstart += st ? 1 : 0;
             }
-        } else {
-            for (int gi = warp; gi < ng; gi += kWarps) {
-                if (prm.groups[gi].gradient)
-                    run_group<ORDER, TILE, true>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
-                else
-                    run_group<ORDER, TILE, false>(prm, box_smem, prep, srcs, cs, gi, origin, it.begin, 0, len, lane);
+            // block exclusive scan of nstart
+            int x = nstart;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) warp_sums[warp] = x;
+            __syncthreads();
+            int wp = 0;
+            for (int w2 = 0; w2 < warp; ++w2) wp += warp_sums[w2];
+            int pos = wp + x - nstart;
+#pragma unroll
+            for (int q = 0; q < PER; ++q)
+                if (flags & (1 << q)) runs[pos++] = threadIdx.x * PER + q;
+            if (threadIdx.x == kThreads - 1) {
+                n_runs = pos;
+                runs[pos] = len;
+            }
+        }
+        __syncthreads();
+        {
+            const int nr = n_runs;
+            if (ng <= kWarps) {
+                const int gi = warp_group[warp];
+                if (gi >= 0) {
+                    if (prm.groups[gi].gradient)
+                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                                                        origin, it.begin, lane);
+                    else
+                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                                                         origin, it.begin, lane);
+                }
+            } else {
+                for (int gi = warp; gi < ng; gi += kWarps) {
+                    if (prm.groups[gi].gradient)
+                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                                                        origin, it.begin, lane);
+                    else
+                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                                                         origin, it.begin, lane);
+                }
             }
         }
         __syncthreads();
