@@ -259,15 +259,19 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
 }
 
-// One warp of channel group gi pulls cell runs of the current item from the
-// group's shared counter until none are left. prep[i] = (u0, u1, u2, key) of
-// item particle i; srcs[s * kChunk + i] is raw source s of item particle i;
-// runs[r] is the first particle of run r (runs[n_runs] = item length).
+// One warp of channel group gi first pulls big cell runs (long runs of one
+// base node inside the box) from the group's shared counter and accumulates
+// each in registers, then pulls the aligned 32-particle windows that hold
+// particles of short runs (or of stencils outside the box) and adds those
+// particles directly. prep[i] = (u0, u1, u2, key) of item particle i;
+// srcs[s * kChunk + i] is raw source s of item particle i; runs[r] is the
+// first particle of run r (runs[n_runs] = item length).
 template <int ORDER, int TILE, bool GRAD>
 __device__ __forceinline__ void process_runs(const TiledParams& prm, float* box_smem, const float4* prep,
-                                             const float* srcs, const int* runs, int n_runs, int* next_run,
-                                             const ChanSmem* cs, int gi, const int* origin, int64_t item_begin,
-                                             int lane) {
+                                             const float* srcs, const int* runs, const int* big, int n_big,
+                                             const unsigned char* direct, const unsigned* win_mask, int n_win,
+                                             int* next, const ChanSmem* cs, int gi, const int* origin,
+                                             int64_t item_begin, int lane) {
     using SH = P2GShape<ORDER>;
     constexpr int BB = TILE + ORDER;
     constexpr int K = SH::K;
@@ -285,61 +289,80 @@ __device__ __forceinline__ void process_runs(const TiledParams& prm, float* box_
             srow[c][n] = c < count ? prm.channels[first + c].src[n] : -1;
             smul[c][n] = srow[c][n] >= 0 ? prm.sources[srow[c][n]].mult : 0.0f;
         }
+    auto load_coef = [&](int i, bool active, float (*coef)[3]) {
+#pragma unroll
+        for (int c = 0; c < CH; ++c)
+#pragma unroll
+            for (int n = 0; n < 3; ++n) {
+                const int rr = n < NS ? srow[c][n < NS ? n : 0] : -1;
+                coef[c][n] = (rr >= 0 && active) ? srcs[rr * kChunk + i] * smul[c][n < NS ? n : 0] : 0.0f;
+            }
+    };
 
     float acc[NPAD];
 #pragma unroll
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
 
+    // Big runs: register accumulation, one flush per run (or per
+    // kMaxRunWindows windows).
     while (true) {
         int r = 0;
-        if (lane == 0) r = atomicAdd(next_run, 1);
+        if (lane == 0) r = atomicAdd(next, 1);
         r = __shfl_sync(0xffffffffu, r, 0);
-        if (r >= n_runs) break;
-        const int rb = runs[r], re = runs[r + 1];
+        if (r >= n_big) break;
+        const int rb = runs[big[r]], re = runs[big[r] + 1];
         const int key = __float_as_int(prep[rb].w);
-        if (key == kKeyInvalid) continue;
-        const bool big = key >= 0 && re - rb >= kSmallRun;
         int windows = 0;
         for (int w0 = rb; w0 < re; w0 += 32) {
             const int i = w0 + lane;
             const bool active = i < re;
             float coef[CH][3];
-#pragma unroll
-            for (int c = 0; c < CH; ++c)
-#pragma unroll
-                for (int n = 0; n < 3; ++n) {
-                    const int rr = n < NS ? srow[c][n < NS ? n : 0] : -1;
-                    coef[c][n] = (rr >= 0 && active) ? srcs[rr * kChunk + i] * smul[c][n < NS ? n : 0] : 0.0f;
-                }
+            load_coef(i, active, coef);
             const float4 pu = active ? prep[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const float u[3] = {pu.x, pu.y, pu.z};
             float w[3][K], g[3][K];
 #pragma unroll
             for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
-            if (big) {
-                if (windows == kMaxRunWindows) {
-                    flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
-                    windows = 0;
-                }
-                ++windows;
-                accumulate<ORDER, CH, GRAD>(acc, w, g, coef, active);
-            } else if (active) {
-                int l[3], s[3];
-                const bool inbox = key >= 0;
-                if (inbox) {
-                    l[2] = key % BB;
-                    l[1] = (key / BB) % BB;
-                    l[0] = key / (BB * BB);
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) s[d] = origin[d] + l[d];
-                } else {
-                    float uu[3];
-                    form_point<ORDER>(prm, item_begin + i, s, uu);
-                }
-                add_direct<ORDER, TILE, CH, GRAD>(prm, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
+            if (windows == kMaxRunWindows) {
+                flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
+                windows = 0;
             }
+            ++windows;
+            accumulate<ORDER, CH, GRAD>(acc, w, g, coef, active);
         }
-        if (big) flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
+        flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
+    }
+    // Windows with particles of short runs: each lane adds its own particle.
+    while (true) {
+        int wi = 0;
+        if (lane == 0) wi = atomicAdd(next + 1, 1);
+        wi = __shfl_sync(0xffffffffu, wi, 0);
+        if (wi >= n_win) break;
+        if (!(win_mask[wi >> 5] & (1u << (wi & 31)))) continue;
+        const int i = wi * 32 + lane;
+        const bool active = direct[i] != 0;
+        float coef[CH][3];
+        load_coef(i, active, coef);
+        if (!active) continue;
+        const float4 pu = prep[i];
+        const int key = __float_as_int(pu.w);
+        const float u[3] = {pu.x, pu.y, pu.z};
+        float w[3][K], g[3][K];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+        int l[3], s[3];
+        const bool inbox = key >= 0;
+        if (inbox) {
+            l[2] = key % BB;
+            l[1] = (key / BB) % BB;
+            l[0] = key / (BB * BB);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) s[d] = origin[d] + l[d];
+        } else {
+            float uu[3];
+            form_point<ORDER>(prm, item_begin + i, s, uu);
+        }
+        add_direct<ORDER, TILE, CH, GRAD>(prm, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
     }
 }
 
@@ -355,8 +378,11 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     __shared__ ChanSmem cs[kMaxChannels];
     __shared__ int item_idx;
     __shared__ int runs[kChunk + 1];
-    __shared__ int n_runs;
-    __shared__ int next_run[kMaxGroups];
+    __shared__ int big[kChunk];
+    __shared__ unsigned char direct[kChunk];
+    __shared__ unsigned win_mask[kChunk / 32 / 32 + 1];
+    __shared__ int n_runs, n_big;
+    __shared__ int next_run[2 * kMaxGroups];
     __shared__ int warp_sums[kWarps];
     __shared__ int warp_group[kWarps], group_warps[kMaxGroups];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -390,7 +416,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     const int64_t nwork = *prm.work_count;
     while (true) {
         if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
-        if (threadIdx.x < kMaxGroups) next_run[threadIdx.x] = 0;
+        if (threadIdx.x < 2 * kMaxGroups) next_run[threadIdx.x] = 0;
+        if (threadIdx.x < kChunk / 32 / 32 + 1) win_mask[threadIdx.x] = 0u;
+        if (threadIdx.x == 0) n_big = 0;
         for (int i = threadIdx.x * 4; i < prm.smem_floats; i += blockDim.x * 4) {
             if (i + 3 < prm.smem_floats)
                 *reinterpret_cast<float4*>(box_smem + i) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -496,25 +524,39 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             }
         }
         __syncthreads();
+        // Classify runs: long runs inside the box go to the big list, the
+        // particles of the others are added directly, window by window.
+        for (int r = threadIdx.x; r < n_runs; r += blockDim.x) {
+            const int rb = runs[r], re = runs[r + 1];
+            const int key = __float_as_int(prep[rb].w);
+            const bool is_big = key >= 0 && re - rb >= kSmallRun;
+            if (is_big) big[atomicAdd(&n_big, 1)] = r;
+            const unsigned char dflag = (!is_big && key != kKeyInvalid) ? 1 : 0;
+            for (int i = rb; i < re; ++i) direct[i] = dflag;
+            if (dflag)
+                for (int wi = rb >> 5; wi <= (re - 1) >> 5; ++wi) atomicOr(&win_mask[wi >> 5], 1u << (wi & 31));
+        }
+        for (int i = len + threadIdx.x; i < ((len + 31) & ~31); i += blockDim.x) direct[i] = 0;
+        __syncthreads();
         {
-            const int nr = n_runs;
+            const int nbig = n_big, nwin = (len + 31) >> 5;
             if (ng <= kWarps) {
                 const int gi = warp_group[warp];
                 if (gi >= 0) {
                     if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                         origin, it.begin, lane);
                     else
-                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                          origin, it.begin, lane);
                 }
             } else {
                 for (int gi = warp; gi < ng; gi += kWarps) {
                     if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                         origin, it.begin, lane);
                     else
-                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, nr, next_run + gi, cs, gi,
+                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                          origin, it.begin, lane);
                 }
             }
