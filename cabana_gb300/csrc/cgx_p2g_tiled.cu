@@ -6,28 +6,29 @@
 // warp's lanes hit one address -- which is exactly what happens when the
 // particles of a warp share a cell:
 //
-//  * A work item is a tile and a contiguous run (<= 4096) of its particles.
-//    A prep pass over the item forms, once per particle, the stencil base
-//    node inside the tile's node box and the FP32 in-cell offsets (one double
-//    FMA per dimension plus integer operations) and keeps them in shared
-//    memory.
+//  * A work item is a tile and a contiguous run (<= 2048) of its particles.
+//    A prep pass stages the operator inputs in shared memory with
+//    asynchronous copies and forms, once per particle, the stencil base node
+//    inside the tile's node box and the FP32 in-cell offsets (one double FMA
+//    per dimension plus integer operations). It then lists the runs of
+//    particles sharing a base node.
 //  * Operators are lowered to channels: one grid dof that receives, per
 //    point, a * W (value channel) or b . grad W (gradient channel). Channels
-//    are grouped (4 value or 3 gradient channels per group for the quadratic
-//    spline) and warps are shared out among the groups in proportion to
-//    their arithmetic, so a lane holds its group's whole stencil
-//    (27 nodes x channels) in registers.
-//  * A warp walks its share of the item 32 particles at a time. While the
-//    lanes of a window hold at most two runs of equal base nodes, each lane
-//    adds its particle into its registers (lanes outside the current run add
-//    zeros); when the base node changes the warp reduces the registers across
+//    are grouped (2 value or 1 gradient channel per group for the quadratic
+//    spline) and the CTA's 16 warps are shared out among the groups in
+//    proportion to their arithmetic, so a lane holds its group's whole
+//    stencil (27 nodes x channels) in registers.
+//  * Warps pull long runs from a shared counter. A run is walked 32 particles
+//    at a time, one particle per lane, each lane adding its particle into its
+//    registers; at the end of the run the warp reduces the registers across
 //    lanes with a transpose-reduction (each lane ends with 1/32 of the sums)
-//    and adds them into the box with compensated shared atomics.
-//  * Windows holding three or more runs add each particle directly with
-//    compensated shared atomics, each lane starting its stencil walk at a
-//    different node so lanes of one cell do not collide; points outside the
-//    box go to global memory with bounds checks, so the tile ordering never
-//    changes the result.
+//    and adds them into the box with compensated shared atomics -- one shared
+//    atomic per node and channel per run instead of one per particle.
+//  * Particles of short runs (and of stencils outside the box) are packed in
+//    aligned 32-particle windows and added directly, each lane walking its
+//    stencil from a different node so lanes of one cell do not collide;
+//    outside the box they go to global memory with bounds checks, so the tile
+//    ordering never changes the result.
 //  * At the end of a work item the box is flushed to the Array, one atomic
 //    per touched node and dof, sum and compensation rounded once.
 #include "cgx_kernels.cuh"
@@ -36,7 +37,7 @@ namespace cgx {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 2048;        // particles per work item (host builds items of this size)
 constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
@@ -48,8 +49,10 @@ template <int ORDER>
 struct P2GShape {
     static constexpr int K = ORDER + 1;
     static constexpr int NODES = K * K * K;
-    static constexpr int CV = ORDER >= 3 ? 2 : 4;  // value channels per group
-    static constexpr int CG = ORDER >= 3 ? 1 : 3;  // gradient channels per group
+    // Channels per group, sized so a lane's stencil sums fit in <= 128
+    // registers (16 warps per SM).
+    static constexpr int CV = ORDER >= 3 ? 1 : (ORDER == 2 ? 2 : 4);  // value channels per group
+    static constexpr int CG = ORDER >= 2 ? 1 : 3;                     // gradient channels per group
     static constexpr int pad32(int v) { return (v + 31) / 32 * 32; }
     static constexpr int NV = pad32(NODES * CV);
     static constexpr int NG = pad32(NODES * CG);
