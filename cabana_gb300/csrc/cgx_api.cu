@@ -496,6 +496,12 @@ const char* cgx_last_error(void) { return g_last_error.c_str(); }
 
 const char* cgx_version(void) { return "cgx 0.1 (sm_103a)"; }
 
+}  // extern "C"
+
+void cgx::set_last_error(const char* msg) { g_last_error = msg; }
+
+extern "C" {
+
 int cgx_last_dispatch(cgx_handle h) { return h ? h->last_dispatch : CGX_DISPATCH_NONE; }
 
 cgx_status cgx_p2g(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point, int spline_order,

@@ -106,6 +106,9 @@ struct TiledParams {
     Source sources[kMaxSources];
 };
 
+// Message returned by cgx_last_error() on this thread.
+void set_last_error(const char* msg);
+
 cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64, int sms, cudaStream_t st);
 cudaError_t launch_halo(const HaloParams& h, bool scatter, int sms, cudaStream_t st);
 cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st);

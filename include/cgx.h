@@ -235,6 +235,29 @@ cgx_status cgx_bin_by_key(cgx_handle h, const int32_t* keys, int64_t begin,
                           uint64_t* offsets, uint64_t* permutes, void* stream);
 
 /*
+ * cgx_bin_by_key without any device allocation (no counterpart in the
+ * reference). Same results as cgx_bin_by_key, for callers that may not let a
+ * library allocate device memory: hosts whose device memory is owned and
+ * budgeted by another allocator, or latency-bound loops where an allocation
+ * (which can synchronise the device) is not allowed. Needs no handle.
+ *
+ * Its scratch is a fixed 6 MiB device array compiled into libcgx, held by
+ * every GPU that loads the library until the process exits. Limits:
+ * end - begin <= CGX_STATIC_MAX_KEYS and nbin <= CGX_STATIC_MAX_BINS; larger
+ * problems return CGX_ERR_INVALID_ARG (use cgx_bin_by_key). The first call on
+ * a device (with that device current) looks up the array's device address;
+ * make that first call before any stream capture. All calls on a device
+ * share the array: calls that overlap on the GPU race, so serialise them.
+ * The call synchronises `stream` to report keys outside [0, nbin).
+ */
+#define CGX_STATIC_MAX_KEYS 262144
+#define CGX_STATIC_MAX_BINS 1048576
+cgx_status cgx_bin_by_key_static(const int32_t* keys, int64_t begin,
+                                 int64_t end, int32_t nbin, int32_t* counts,
+                                 uint64_t* offsets, uint64_t* permutes,
+                                 void* stream);
+
+/*
  * permute(BinningData, AoSoA/Slice/View) (core/src/Cabana_Sort.hpp:549-720):
  * for each field, element i in [begin, end) becomes old element
  * permutes[i - begin], all components (ncomps[f] of them) moved together.
