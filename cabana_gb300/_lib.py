@@ -24,6 +24,10 @@ CGX_CELL = 1
 CGX_PLAIN_FP64 = 0
 CGX_FP32_COMPENSATED = 1
 
+# transposed tensor operators (no reference counterpart; used by the adjoints)
+CGX_TENSOR_DIVERGENCE_T_P2G = 5
+CGX_VECTOR_GRADIENT_T_G2P = 5
+
 CGX_FLAG_SKIP_HALO = 1
 CGX_FLAG_CHECK_BOUNDS = 2
 
@@ -34,7 +38,7 @@ CGX_DISPATCH_TILED = 2
 
 EXPORTS = (
     "cgx_create", "cgx_destroy", "cgx_last_error", "cgx_version", "cgx_last_dispatch",
-    "cgx_p2g", "cgx_g2p", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
+    "cgx_p2g", "cgx_g2p", "cgx_p2g_adjoint", "cgx_g2p_adjoint", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
     "cgx_cartesian_num_bins", "cgx_linked_cell_build", "cgx_bin_by_key", "cgx_bin_by_key_static", "cgx_permute",
     "cgx_tiling_init", "cgx_tiling_num_offsets", "cgx_sort_tiles",
 )
@@ -79,6 +83,18 @@ class CgxOp(ctypes.Structure):
     ]
 
 
+class CgxAdjointOp(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("multiplier", ctypes.c_double),
+        ("x", CgxField),
+        ("x_bar", CgxField),
+        ("array", CgxArray),
+        ("array_bar", CgxArray),
+    ]
+
+
 class CgxTiling(ctypes.Structure):
     _fields_ = [
         ("tile", ctypes.c_int32 * 3),
@@ -118,6 +134,10 @@ def lib():
               P(CgxTiling), ctypes.c_uint, vp]
     L.cgx_p2g.argtypes = interp
     L.cgx_g2p.argtypes = interp
+    adj = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, ctypes.c_int, P(CgxAdjointOp), ctypes.c_int, ctypes.c_int,
+           P(CgxTiling), P(CgxField), ctypes.c_uint, vp]
+    L.cgx_p2g_adjoint.argtypes = adj
+    L.cgx_g2p_adjoint.argtypes = adj
     L.cgx_halo_scatter_sum.argtypes = [P(CgxMesh), P(CgxArray), vp]
     L.cgx_halo_gather.argtypes = [P(CgxMesh), P(CgxArray), vp]
     L.cgx_array_assign.argtypes = [P(CgxMesh), P(CgxArray), ctypes.c_double, vp]

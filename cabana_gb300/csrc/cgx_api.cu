@@ -115,14 +115,15 @@ int p2g_comps(int kind) {
     switch (kind) {
         case CGX_SCALAR_VALUE_P2G: case CGX_SCALAR_GRADIENT_P2G: return 1;
         case CGX_VECTOR_VALUE_P2G: case CGX_VECTOR_DIVERGENCE_P2G: return 3;
-        case CGX_TENSOR_DIVERGENCE_P2G: return 9;
+        case CGX_TENSOR_DIVERGENCE_P2G: case CGX_TENSOR_DIVERGENCE_T_P2G: return 9;
     }
     return -1;
 }
 int p2g_dofs(int kind) {
     switch (kind) {
         case CGX_SCALAR_VALUE_P2G: case CGX_VECTOR_DIVERGENCE_P2G: return 1;
-        case CGX_VECTOR_VALUE_P2G: case CGX_SCALAR_GRADIENT_P2G: case CGX_TENSOR_DIVERGENCE_P2G: return 3;
+        case CGX_VECTOR_VALUE_P2G: case CGX_SCALAR_GRADIENT_P2G: case CGX_TENSOR_DIVERGENCE_P2G:
+        case CGX_TENSOR_DIVERGENCE_T_P2G: return 3;
     }
     return -1;
 }
@@ -130,14 +131,15 @@ int g2p_comps(int kind) {
     switch (kind) {
         case CGX_SCALAR_VALUE_G2P: case CGX_VECTOR_DIVERGENCE_G2P: return 1;
         case CGX_VECTOR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 3;
-        case CGX_VECTOR_GRADIENT_G2P: return 9;
+        case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_GRADIENT_T_G2P: return 9;
     }
     return -1;
 }
 int g2p_dofs(int kind) {
     switch (kind) {
         case CGX_SCALAR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 1;
-        case CGX_VECTOR_VALUE_G2P: case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_DIVERGENCE_G2P: return 3;
+        case CGX_VECTOR_VALUE_G2P: case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_DIVERGENCE_G2P:
+        case CGX_VECTOR_GRADIENT_T_G2P: return 3;
     }
     return -1;
 }
@@ -188,13 +190,13 @@ cgx_status finish_check(cgx_context* h, unsigned flags, cudaStream_t st) {
     return CGX_OK;
 }
 
-cgx_status halo_all(const cgx_mesh& m, const cgx_op* ops, int n_ops, bool scatter, int sms, cudaStream_t st) {
+cgx_status halo_all(const cgx_mesh& m, const cgx_op* ops, int n_ops, int mode, int sms, cudaStream_t st) {
     if (!any_periodic(m)) return CGX_OK;
     for (int o = 0; o < n_ops; ++o) {
         bool seen = false;
         for (int q = 0; q < o; ++q) seen |= ops[q].array.data == ops[o].array.data;
         if (seen) continue;
-        CGX_CUDA(launch_halo(to_halo(m, ops[o].array), scatter, sms, st));
+        CGX_CUDA(launch_halo(to_halo(m, ops[o].array), mode, sms, st));
     }
     return CGX_OK;
 }
@@ -207,6 +209,7 @@ cgx_status halo_all(const cgx_mesh& m, const cgx_op* ops, int n_ops, bool scatte
 //   ScalarGradientP2G   -> 3 gradient channels  b = m f e_d
 //   VectorDivergenceP2G -> 1 gradient channel   b = m f
 //   TensorDivergenceP2G -> 3 gradient channels  b = m f_{d,:}
+//   (transposed form)   -> 3 gradient channels  b = m f_{:,d}
 bool plan_channels(TiledParams& prm, const cgx_op* ops, int n_ops, int order) {
     Channel val[kMaxChannels], grd[kMaxChannels];
     int nv = 0, ng = 0;
@@ -267,6 +270,12 @@ bool plan_channels(TiledParams& prm, const cgx_op* ops, int n_ops, int order) {
             case CGX_TENSOR_DIVERGENCE_P2G:
                 for (int m = 0; m < 3; ++m) {
                     const int c[3] = {3 * m, 3 * m + 1, 3 * m + 2};
+                    add(true, slot, m, o, c);
+                }
+                break;
+            case CGX_TENSOR_DIVERGENCE_T_P2G:
+                for (int m = 0; m < 3; ++m) {
+                    const int c[3] = {m, 3 + m, 6 + m};
                     add(true, slot, m, o, c);
                 }
                 break;
@@ -345,7 +354,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
 
     const DMesh dm = to_dmesh(*mesh);
     if (!p2g && !(flags & CGX_FLAG_SKIP_HALO)) {
-        s = halo_all(*mesh, ops, n_ops, false, h->sms, st);
+        s = halo_all(*mesh, ops, n_ops, kHaloGather, h->sms, st);
         if (s) return s;
     }
 
@@ -447,8 +456,183 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
         h->last_dispatch = CGX_DISPATCH_POINTS;
     }
     if (p2g && !(flags & CGX_FLAG_SKIP_HALO)) {
-        s = halo_all(*mesh, ops, n_ops, true, h->sms, st);
+        s = halo_all(*mesh, ops, n_ops, kHaloScatterSum, h->sms, st);
         if (s) return s;
+    }
+    return finish_check(h, flags, st);
+}
+
+// Pairing of point field and grid array in the position adjoint of a
+// forward operator (see cgx_adjoint.cu); -1 for an unknown kind.
+int adjoint_pattern(int kind, bool p2g) {
+    if (p2g) {
+        switch (kind) {
+            case CGX_SCALAR_VALUE_P2G: return kAdjValue1;
+            case CGX_VECTOR_VALUE_P2G: return kAdjValue3;
+            case CGX_SCALAR_GRADIENT_P2G: return kAdjGradA;
+            case CGX_VECTOR_DIVERGENCE_P2G: return kAdjGradS;
+            case CGX_TENSOR_DIVERGENCE_P2G: return kAdjTensor;
+            case CGX_TENSOR_DIVERGENCE_T_P2G: return kAdjTensorT;
+        }
+    } else {
+        switch (kind) {
+            case CGX_SCALAR_VALUE_G2P: return kAdjValue1;
+            case CGX_VECTOR_VALUE_G2P: return kAdjValue3;
+            case CGX_SCALAR_GRADIENT_G2P: return kAdjGradS;
+            case CGX_VECTOR_GRADIENT_G2P: return kAdjTensorT;
+            case CGX_VECTOR_DIVERGENCE_G2P: return kAdjGradA;
+            case CGX_VECTOR_GRADIENT_T_G2P: return kAdjTensor;
+        }
+    }
+    return -1;
+}
+
+// The operator of the other direction whose linear map is the transpose of
+// a forward operator's (same multiplier): the value part of its adjoint.
+int transpose_kind(int kind, bool p2g) {
+    if (p2g) {
+        switch (kind) {
+            case CGX_SCALAR_VALUE_P2G: return CGX_SCALAR_VALUE_G2P;
+            case CGX_VECTOR_VALUE_P2G: return CGX_VECTOR_VALUE_G2P;
+            case CGX_SCALAR_GRADIENT_P2G: return CGX_VECTOR_DIVERGENCE_G2P;
+            case CGX_VECTOR_DIVERGENCE_P2G: return CGX_SCALAR_GRADIENT_G2P;
+            case CGX_TENSOR_DIVERGENCE_P2G: return CGX_VECTOR_GRADIENT_T_G2P;
+            case CGX_TENSOR_DIVERGENCE_T_P2G: return CGX_VECTOR_GRADIENT_G2P;
+        }
+    } else {
+        switch (kind) {
+            case CGX_SCALAR_VALUE_G2P: return CGX_SCALAR_VALUE_P2G;
+            case CGX_VECTOR_VALUE_G2P: return CGX_VECTOR_VALUE_P2G;
+            case CGX_SCALAR_GRADIENT_G2P: return CGX_VECTOR_DIVERGENCE_P2G;
+            case CGX_VECTOR_GRADIENT_G2P: return CGX_TENSOR_DIVERGENCE_T_P2G;
+            case CGX_VECTOR_DIVERGENCE_G2P: return CGX_SCALAR_GRADIENT_P2G;
+            case CGX_VECTOR_GRADIENT_T_G2P: return CGX_TENSOR_DIVERGENCE_P2G;
+        }
+    }
+    return -1;
+}
+
+cgx_status check_array(const cgx_array& a, int dofs, const char* what) {
+    if (!a.data) return fail(CGX_ERR_INVALID_ARG, std::string(what) + ".data is NULL");
+    if (!valid_dtype(a.dtype)) return fail(CGX_ERR_INVALID_ARG, std::string(what) + ".dtype must be CGX_F32 or CGX_F64");
+    if (a.dofs < dofs) return fail(CGX_ERR_INVALID_ARG, std::string(what) + " has fewer dofs than the operator uses");
+    return CGX_OK;
+}
+
+// cgx_p2g_adjoint (p2g = true) and cgx_g2p_adjoint (p2g = false).
+cgx_status adjoint(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point, int spline_order,
+                   const cgx_adjoint_op* ops, int n_ops, int precision, const cgx_tiling* tiling,
+                   const cgx_field* points_bar, unsigned flags, void* stream, bool p2g) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    if (num_point < 0) return fail(CGX_ERR_INVALID_ARG, "num_point must be >= 0");
+    if (num_point > 0) {
+        s = check_field(points, "points");
+        if (s) return s;
+        if (points->dtype != CGX_F64) return fail(CGX_ERR_INVALID_ARG, "point coordinates must be double (CGX_F64)");
+    }
+    if (spline_order < 0 || spline_order > 6) return fail(CGX_ERR_NOT_SUPPORTED, "spline order must be in [0, 6]");
+    if (precision != CGX_PLAIN_FP64 && precision != CGX_FP32_COMPENSATED)
+        return fail(CGX_ERR_INVALID_ARG, "unknown precision");
+    if (!ops || n_ops < 1 || n_ops > kMaxOps) return fail(CGX_ERR_INVALID_ARG, "n_ops must be in [1, 8]");
+    const bool want_pos = points_bar != nullptr;
+    if (want_pos && num_point > 0) {
+        s = check_field(points_bar, "points_bar");
+        if (s) return s;
+    }
+    // Validate every operator for the roles it plays in this call.
+    for (int o = 0; o < n_ops; ++o) {
+        const cgx_adjoint_op& op = ops[o];
+        if (adjoint_pattern(op.kind, p2g) < 0) return fail(CGX_ERR_INVALID_ARG, "unknown operator kind");
+        const int dofs = p2g ? p2g_dofs(op.kind) : g2p_dofs(op.kind);
+        if (p2g) {
+            s = check_array(op.array_bar, dofs, "op.array_bar");
+            if (s) return s;
+            if (num_point > 0 && op.x_bar.data) {
+                s = check_field(&op.x_bar, "op.x_bar");
+                if (s) return s;
+            }
+            if (num_point > 0 && want_pos) {
+                s = check_field(&op.x, "op.x");
+                if (s) return s;
+            }
+        } else {
+            if (num_point > 0) {
+                s = check_field(&op.x_bar, "op.x_bar");
+                if (s) return s;
+            }
+            if (op.array_bar.data) {
+                s = check_array(op.array_bar, dofs, "op.array_bar");
+                if (s) return s;
+            }
+            if (want_pos) {
+                s = check_array(op.array, dofs, "op.array");
+                if (s) return s;
+            }
+        }
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (flags & CGX_FLAG_CHECK_BOUNDS) CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
+    const unsigned inner = (flags & ~CGX_FLAG_CHECK_BOUNDS) | CGX_FLAG_SKIP_HALO;
+    const bool halo = any_periodic(*mesh) && !(flags & CGX_FLAG_SKIP_HALO);
+
+    // The value part is the transposed operator through the forward kernels.
+    cgx_op vops[kMaxOps];
+    int nv = 0;
+    for (int o = 0; o < n_ops; ++o) {
+        const cgx_adjoint_op& op = ops[o];
+        if (p2g ? !op.x_bar.data : !op.array_bar.data) continue;
+        cgx_op& v = vops[nv++];
+        std::memset(&v, 0, sizeof(v));
+        v.kind = transpose_kind(op.kind, p2g);
+        v.multiplier = op.multiplier;
+        v.x = op.x_bar;
+        v.array = op.array_bar;
+    }
+
+    if (p2g && halo) {
+        // adjoint of the forward halo scatter(Sum), on each distinct array_bar
+        for (int o = 0; o < n_ops; ++o) {
+            bool seen = false;
+            for (int q = 0; q < o; ++q) seen |= ops[q].array_bar.data == ops[o].array_bar.data;
+            if (!seen) CGX_CUDA(launch_halo(to_halo(*mesh, ops[o].array_bar), kHaloGatherAdd, h->sms, st));
+        }
+    }
+    if (want_pos && num_point > 0) {
+        AdjointParams prm;
+        std::memset(&prm, 0, sizeof(prm));
+        prm.mesh = to_dmesh(*mesh);
+        prm.points = to_dfield(*points);
+        prm.points_bar = to_dfield(*points_bar);
+        prm.num_point = num_point;
+        prm.n_terms = n_ops;
+        prm.error_flag = h->flags;
+        for (int o = 0; o < n_ops; ++o) {
+            AdjointTerm& t = prm.terms[o];
+            t.pattern = adjoint_pattern(ops[o].kind, p2g);
+            t.mult = ops[o].multiplier;
+            t.mult_f = float(ops[o].multiplier);
+            const cgx_field& sf = p2g ? ops[o].x : ops[o].x_bar;
+            const cgx_array& af = p2g ? ops[o].array_bar : ops[o].array;
+            t.s = to_dfield(sf);
+            t.a.data = reinterpret_cast<char*>(af.data);
+            t.a.dtype = af.dtype;
+            t.a.dofs = af.dofs;
+        }
+        CGX_CUDA(launch_adjoint_points(prm, spline_order, precision == CGX_PLAIN_FP64, h->sms, st));
+    }
+    if (nv > 0 && num_point > 0) {
+        s = interpolate(h, mesh, points, num_point, spline_order, vops, nv, precision, tiling, inner, stream, !p2g);
+        if (s) return s;
+    }
+    if (!p2g && halo) {
+        // adjoint of the forward halo gather, on each distinct array_bar
+        for (int o = 0; o < nv; ++o) {
+            bool seen = false;
+            for (int q = 0; q < o; ++q) seen |= vops[q].array.data == vops[o].array.data;
+            if (!seen) CGX_CUDA(launch_halo(to_halo(*mesh, vops[o].array), kHaloScatterClear, h->sms, st));
+        }
     }
     return finish_check(h, flags, st);
 }
@@ -516,6 +700,20 @@ cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, 
     return interpolate(h, mesh, points, num_point, spline_order, ops, n_ops, precision, tiling, flags, stream, false);
 }
 
+cgx_status cgx_p2g_adjoint(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point,
+                           int spline_order, const cgx_adjoint_op* ops, int n_ops, int precision,
+                           const cgx_tiling* tiling, const cgx_field* points_bar, unsigned flags, void* stream) {
+    return adjoint(h, mesh, points, num_point, spline_order, ops, n_ops, precision, tiling, points_bar, flags, stream,
+                   true);
+}
+
+cgx_status cgx_g2p_adjoint(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point,
+                           int spline_order, const cgx_adjoint_op* ops, int n_ops, int precision,
+                           const cgx_tiling* tiling, const cgx_field* points_bar, unsigned flags, void* stream) {
+    return adjoint(h, mesh, points, num_point, spline_order, ops, n_ops, precision, tiling, points_bar, flags, stream,
+                   false);
+}
+
 cgx_status cgx_halo_scatter_sum(const cgx_mesh* mesh, const cgx_array* array, void* stream) {
     cgx_status s = check_mesh(mesh);
     if (s) return s;
@@ -525,7 +723,7 @@ cgx_status cgx_halo_scatter_sum(const cgx_mesh* mesh, const cgx_array* array, vo
     int dev = 0, sms = 0;
     CGX_CUDA(cudaGetDevice(&dev));
     CGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CGX_CUDA(launch_halo(to_halo(*mesh, *array), true, sms, reinterpret_cast<cudaStream_t>(stream)));
+    CGX_CUDA(launch_halo(to_halo(*mesh, *array), kHaloScatterSum, sms, reinterpret_cast<cudaStream_t>(stream)));
     return CGX_OK;
 }
 
@@ -538,7 +736,7 @@ cgx_status cgx_halo_gather(const cgx_mesh* mesh, const cgx_array* array, void* s
     int dev = 0, sms = 0;
     CGX_CUDA(cudaGetDevice(&dev));
     CGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CGX_CUDA(launch_halo(to_halo(*mesh, *array), false, sms, reinterpret_cast<cudaStream_t>(stream)));
+    CGX_CUDA(launch_halo(to_halo(*mesh, *array), kHaloGather, sms, reinterpret_cast<cudaStream_t>(stream)));
     return CGX_OK;
 }
 

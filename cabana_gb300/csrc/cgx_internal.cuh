@@ -203,6 +203,36 @@ struct SplineKernel {
             }
         }
     }
+
+    // Second derivatives of the knot weights with respect to the physical
+    // coordinate (r2 = rdx^2): the derivative of `weights`' gradient. For
+    // degree n, d2/du2 B_n = B_{n-2}[a-2] - 2 B_{n-2}[a-1] + B_{n-2}[a].
+    // Orders 0 and 1 are piecewise constant / linear: zero almost everywhere.
+    __device__ __forceinline__ static void hessian(T u, T r2, T* h) {
+        if constexpr (ORDER <= 1) {
+#pragma unroll
+            for (int a = 0; a < nk; ++a) h[a] = T(0);
+        } else if constexpr (ORDER == 2) {
+            h[0] = r2;
+            h[1] = T(-2) * r2;
+            h[2] = r2;
+        } else if constexpr (ORDER == 3) {
+            h[0] = (T(1) - u) * r2;
+            h[1] = (T(3) * u - T(2)) * r2;
+            h[2] = (T(1) - T(3) * u) * r2;
+            h[3] = u * r2;
+        } else {
+            T b[ORDER - 1];
+            de_boor<ORDER - 2, T>(u, b);
+#pragma unroll
+            for (int a = 0; a <= ORDER; ++a) {
+                const T l2 = (a >= 2) ? b[a - 2] : T(0);
+                const T l1 = (a >= 1 && a - 1 <= ORDER - 2) ? b[a - 1] : T(0);
+                const T l0 = (a <= ORDER - 2) ? b[a] : T(0);
+                h[a] = (l2 - T(2) * l1 + l0) * r2;
+            }
+        }
+    }
 };
 
 // Reference mapping in double: x0 = (xp - low) * rdx (+ 0.5 on the dual grid

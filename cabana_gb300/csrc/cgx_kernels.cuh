@@ -106,11 +106,53 @@ struct TiledParams {
     Source sources[kMaxSources];
 };
 
+// One term of the position adjoint: per point,
+//   dL/dx_e += mult * sum_n ( r_n dW_n/dx_e + sum_d q_n[d] d2W_n/(dx_e dx_d) )
+// where r_n and q_n pair the point field `s` with the dofs A of array `a` at
+// node n according to `pattern`.
+enum AdjointPattern : int32_t {
+    kAdjValue1 = 0,   // r = s A0                       (ScalarValue P2G / G2P)
+    kAdjValue3 = 1,   // r = sum_c s_c A_c              (VectorValue P2G / G2P)
+    kAdjGradA = 2,    // q_d = s A_d                    (ScalarGradientP2G, VectorDivergenceG2P)
+    kAdjGradS = 3,    // q_d = s_d A0                   (VectorDivergenceP2G, ScalarGradientG2P)
+    kAdjTensor = 4,   // q_b = sum_a s[a][b] A_a        (TensorDivergenceP2G, transposed VectorGradientG2P)
+    kAdjTensorT = 5,  // q_a = sum_b s[a][b] A_b        (transposed TensorDivergenceP2G, VectorGradientG2P)
+};
+
+struct AdjointTerm {
+    int32_t pattern;
+    float mult_f;
+    double mult;
+    DField s;
+    DArray a;
+};
+
+struct AdjointParams {
+    DMesh mesh;
+    DField points;
+    DField points_bar;
+    int64_t num_point;
+    int32_t n_terms;
+    int32_t reserved;
+    int* error_flag;
+    AdjointTerm terms[kMaxOps];
+};
+
 // Message returned by cgx_last_error() on this thread.
 void set_last_error(const char* msg);
 
+// Halo modes on one rank. Gather / scatter-sum are Halo::gather and
+// Halo::scatter(Sum); the other two are their adjoints (exact transposes).
+enum HaloMode : int {
+    kHaloGather = 0,        // ghost = owned image
+    kHaloScatterSum = 1,    // owned image += ghost
+    kHaloGatherAdd = 2,     // ghost += owned image        (adjoint of scatter-sum)
+    kHaloScatterClear = 3,  // owned image += ghost; ghost = 0   (adjoint of gather)
+};
+
 cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64, int sms, cudaStream_t st);
-cudaError_t launch_halo(const HaloParams& h, bool scatter, int sms, cudaStream_t st);
+cudaError_t launch_adjoint_points(const AdjointParams& prm, int order, bool fp64, int sms, cudaStream_t st);
+cudaError_t launch_halo(const HaloParams& h, int mode, int sms, cudaStream_t st);
 cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st);
 
 // Tiled g2p for the operators reading array `slot` (its node box is staged at

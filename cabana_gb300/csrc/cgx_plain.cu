@@ -101,12 +101,15 @@ __global__ void __launch_bounds__(256) p2g_points_kernel(const __grid_constant__
                             }
                     break;
                 }
-                case CGX_TENSOR_DIVERGENCE_P2G: {
+                case CGX_TENSOR_DIVERGENCE_P2G:
+                case CGX_TENSOR_DIVERGENCE_T_P2G: {
+                    // pd[m][n]: the tensor entry paired with dW/dx_n for grid dof m
+                    const bool tr = op.kind == CGX_TENSOR_DIVERGENCE_T_P2G;
                     T pd[3][3];
 #pragma unroll
                     for (int a = 0; a < 3; ++a)
 #pragma unroll
-                        for (int b = 0; b < 3; ++b) pd[a][b] = mult * load_field<T>(op.x, p, a * 3 + b);
+                        for (int b = 0; b < 3; ++b) pd[a][b] = mult * load_field<T>(op.x, p, tr ? b * 3 + a : a * 3 + b);
 #pragma unroll U
                     for (int i = 0; i < nk; ++i)
 #pragma unroll U
@@ -205,7 +208,10 @@ __global__ void __launch_bounds__(256) g2p_points_kernel(const __grid_constant__
                     for (int d = 0; d < 3; ++d) add_field<T>(op.x, p, d, mult * result[d]);
                     break;
                 }
-                case CGX_VECTOR_GRADIENT_G2P: {
+                case CGX_VECTOR_GRADIENT_G2P:
+                case CGX_VECTOR_GRADIENT_T_G2P: {
+                    // result[a][b] = sum dW/dx_a f_b, stored at (a, b) or transposed at (b, a)
+                    const bool tr = op.kind == CGX_VECTOR_GRADIENT_T_G2P;
                     T result[3][3];
 #pragma unroll
                     for (int a = 0; a < 3; ++a)
@@ -231,7 +237,7 @@ __global__ void __launch_bounds__(256) g2p_points_kernel(const __grid_constant__
 #pragma unroll
                     for (int a = 0; a < 3; ++a)
 #pragma unroll
-                        for (int b = 0; b < 3; ++b) add_field<T>(op.x, p, a * 3 + b, mult * result[a][b]);
+                        for (int b = 0; b < 3; ++b) add_field<T>(op.x, p, tr ? b * 3 + a : a * 3 + b, mult * result[a][b]);
                     break;
                 }
                 case CGX_VECTOR_DIVERGENCE_G2P: {
@@ -282,8 +288,11 @@ __device__ __forceinline__ bool halo_partner(const HaloParams& h, int i, int j, 
     return ghost;
 }
 
-template <class T>
-__global__ void halo_scatter_kernel(const __grid_constant__ HaloParams h) {
+// One thread per entity; only ghosts with an owned image do work. An owned
+// image is never a ghost, so each mode reads and writes disjoint entries
+// except for the atomic sums into owned images.
+template <class T, int MODE>
+__global__ void halo_kernel(const __grid_constant__ HaloParams h) {
     const int64_t total = int64_t(h.ext[0]) * h.ext[1] * h.ext[2];
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     for (int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; n < total; n += stride) {
@@ -293,22 +302,20 @@ __global__ void halo_scatter_kernel(const __grid_constant__ HaloParams h) {
         int64_t own;
         if (!halo_partner(h, i, j, k, own)) continue;
         T* a = reinterpret_cast<T*>(h.data);
-        for (int c = 0; c < h.dofs; ++c) atomicAdd(a + own * h.dofs + c, a[n * h.dofs + c]);
-    }
-}
-
-template <class T>
-__global__ void halo_gather_kernel(const __grid_constant__ HaloParams h) {
-    const int64_t total = int64_t(h.ext[0]) * h.ext[1] * h.ext[2];
-    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-    for (int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; n < total; n += stride) {
-        const int k = int(n % h.ext[2]);
-        const int j = int((n / h.ext[2]) % h.ext[1]);
-        const int i = int(n / (int64_t(h.ext[1]) * h.ext[2]));
-        int64_t own;
-        if (!halo_partner(h, i, j, k, own)) continue;
-        T* a = reinterpret_cast<T*>(h.data);
-        for (int c = 0; c < h.dofs; ++c) a[n * h.dofs + c] = a[own * h.dofs + c];
+        for (int c = 0; c < h.dofs; ++c) {
+            T* ghost = a + n * h.dofs + c;
+            T* image = a + own * h.dofs + c;
+            if constexpr (MODE == kHaloGather) {
+                *ghost = *image;
+            } else if constexpr (MODE == kHaloScatterSum) {
+                atomicAdd(image, *ghost);
+            } else if constexpr (MODE == kHaloGatherAdd) {
+                *ghost += *image;
+            } else {
+                atomicAdd(image, *ghost);
+                *ghost = T(0);
+            }
+        }
     }
 }
 
@@ -358,21 +365,23 @@ cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_halo(const HaloParams& h, bool scatter, int sms, cudaStream_t st) {
-    const int64_t total = int64_t(h.ext[0]) * h.ext[1] * h.ext[2];
-    const int blocks = grid_blocks(total, 256, sms);
-    if (h.dtype == CGX_F64) {
-        if (scatter)
-            halo_scatter_kernel<double><<<blocks, 256, 0, st>>>(h);
-        else
-            halo_gather_kernel<double><<<blocks, 256, 0, st>>>(h);
-    } else {
-        if (scatter)
-            halo_scatter_kernel<float><<<blocks, 256, 0, st>>>(h);
-        else
-            halo_gather_kernel<float><<<blocks, 256, 0, st>>>(h);
+template <class T>
+static cudaError_t launch_halo_t(const HaloParams& h, int mode, int blocks, cudaStream_t st) {
+    switch (mode) {
+        case kHaloGather: halo_kernel<T, kHaloGather><<<blocks, 256, 0, st>>>(h); break;
+        case kHaloScatterSum: halo_kernel<T, kHaloScatterSum><<<blocks, 256, 0, st>>>(h); break;
+        case kHaloGatherAdd: halo_kernel<T, kHaloGatherAdd><<<blocks, 256, 0, st>>>(h); break;
+        case kHaloScatterClear: halo_kernel<T, kHaloScatterClear><<<blocks, 256, 0, st>>>(h); break;
+        default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_halo(const HaloParams& h, int mode, int sms, cudaStream_t st) {
+    const int64_t total = int64_t(h.ext[0]) * h.ext[1] * h.ext[2];
+    const int blocks = grid_blocks(total, 256, sms);
+    if (h.dtype == CGX_F64) return launch_halo_t<double>(h, mode, blocks, st);
+    return launch_halo_t<float>(h, mode, blocks, st);
 }
 
 cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st) {

@@ -36,13 +36,13 @@ int g2p_comps(int kind) {
     switch (kind) {
         case CGX_SCALAR_VALUE_G2P: case CGX_VECTOR_DIVERGENCE_G2P: return 1;
         case CGX_VECTOR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 3;
-        case CGX_VECTOR_GRADIENT_G2P: return 9;
+        case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_GRADIENT_T_G2P: return 9;
     }
     return 0;
 }
 
 __device__ __forceinline__ int dev_g2p_comps(int kind) {
-    return kind == CGX_VECTOR_GRADIENT_G2P ? 9
+    return (kind == CGX_VECTOR_GRADIENT_G2P || kind == CGX_VECTOR_GRADIENT_T_G2P) ? 9
            : (kind == CGX_VECTOR_VALUE_G2P || kind == CGX_SCALAR_GRADIENT_G2P) ? 3 : 1;
 }
 
@@ -168,6 +168,13 @@ __device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, floa
                 for (int a = 0; a < 3; ++a)
 #pragma unroll
                     for (int b = 0; b < 3; ++b) x[(a * 3 + b) * kSub] += mult * D[a][b < NDOF ? b : 0];
+                col += 9;
+                break;
+            case CGX_VECTOR_GRADIENT_T_G2P:
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) x[(b * 3 + a) * kSub] += mult * D[a][b < NDOF ? b : 0];
                 col += 9;
                 break;
             case CGX_VECTOR_DIVERGENCE_G2P:
@@ -364,6 +371,7 @@ void g2p_slot_need(const TiledParams& prm, int slot, int& ndof, bool& grad) {
             case CGX_VECTOR_VALUE_G2P: ndof = 3; break;
             case CGX_SCALAR_GRADIENT_G2P: grad = true; break;
             case CGX_VECTOR_GRADIENT_G2P:
+            case CGX_VECTOR_GRADIENT_T_G2P:
             case CGX_VECTOR_DIVERGENCE_G2P: ndof = 3; grad = true; break;
         }
     }

@@ -306,6 +306,90 @@ def g2p(array, halo: Optional[Halo], points, num_point, spline: Spline, functor,
                             len(fs), precision, til, fl, _stream(stream)))
 
 
+def createTensorDivergenceTransposedP2G(x, multiplier):
+    """TensorDivergenceP2G of the transposed tensor (no reference
+    counterpart): grid_m += sum_n dW/dx_n x[n][m]."""
+    return _mk(L.CGX_TENSOR_DIVERGENCE_T_P2G, x, multiplier, True, 3)
+
+
+def createVectorGradientTransposedG2P(x, multiplier):
+    """VectorGradientG2P stored transposed (no reference counterpart):
+    x[m][n] += multiplier * sum dW/dx_n f_m."""
+    return _mk(L.CGX_VECTOR_GRADIENT_T_G2P, x, multiplier, False, 3)
+
+
+def _null_field():
+    return L.CgxField()
+
+
+def _null_array():
+    return L.CgxArray()
+
+
+def _adjoint_call(fn, functors, points, num_point, spline, halo, xs, x_bars, arrays, array_bars, points_bar,
+                  precision, tiling, handle, stream, check_bounds):
+    n = len(functors)
+    ops = (L.CgxAdjointOp * n)()
+    for i, f in enumerate(functors):
+        ops[i].kind = f.kind
+        ops[i].multiplier = f.multiplier
+        ops[i].x = field_descriptor(xs[i]) if xs[i] is not None else _null_field()
+        ops[i].x_bar = field_descriptor(x_bars[i]) if x_bars[i] is not None else _null_field()
+        ops[i].array = arrays[i].descriptor() if arrays[i] is not None else _null_array()
+        ops[i].array_bar = array_bars[i].descriptor() if array_bars[i] is not None else _null_array()
+    grid_ref = next(a for a in list(array_bars) + list(arrays) if a is not None)
+    mesh = grid_ref.mesh()
+    pts = field_descriptor(points)
+    pb = ctypes.byref(field_descriptor(points_bar)) if points_bar is not None else None
+    h = handle or L.default_handle()
+    fl = (0 if halo is not None else L.CGX_FLAG_SKIP_HALO) | (L.CGX_FLAG_CHECK_BOUNDS if check_bounds else 0)
+    til = ctypes.byref(tiling.struct) if tiling is not None else None
+    L.check(fn(h.ptr, ctypes.byref(mesh), ctypes.byref(pts), int(num_point), spline.order, ops, n, precision, til, pb,
+               fl, _stream(stream)))
+
+
+def p2g_adjoint(functor, points, num_point, spline: Spline, halo: Optional[Halo], array_bar, *, x_bar=None,
+                points_bar=None, precision=PLAIN_FP64, tiling=None, handle=None, stream=None, check_bounds=False):
+    """Reverse mode of p2g (no reference counterpart).
+
+    `functor`: the forward P2G functors; `array_bar`: dL/d(forward array) per
+    functor (read; its ghosts are halo-adjusted in place on periodic meshes
+    when `halo` is given); `x_bar`: tensors receiving dL/d(functor field),
+    added (entries may be None); `points_bar`: (n, 3) tensor receiving
+    dL/d(position), added.
+    """
+    fs, abars = _as_list(functor), _as_list(array_bar)
+    if len(abars) == 1 and len(fs) > 1:
+        abars = abars * len(fs)
+    if any(not f.p2g for f in fs):
+        raise TypeError("p2g_adjoint needs P2G functors")
+    xb = _as_list(x_bar) if x_bar is not None else [None] * len(fs)
+    _adjoint_call(L.lib().cgx_p2g_adjoint, fs, points, num_point, spline, halo, [f.x for f in fs], xb,
+                  [None] * len(fs), abars, points_bar, precision, tiling, handle, stream, check_bounds)
+
+
+def g2p_adjoint(array, halo: Optional[Halo], points, num_point, spline: Spline, functor, x_bar, *, array_bar=None,
+                points_bar=None, precision=PLAIN_FP64, tiling=None, handle=None, stream=None, check_bounds=False):
+    """Reverse mode of g2p (no reference counterpart).
+
+    `array`: the forward arrays as g2p read them; `functor`: the forward G2P
+    functors; `x_bar`: dL/d(functor output field) per functor (read);
+    `array_bar`: Arrays receiving dL/d(array), added (entries may be None);
+    `points_bar`: (n, 3) tensor receiving dL/d(position), added.
+    """
+    fs, arrs = _as_list(functor), _as_list(array)
+    if len(arrs) == 1 and len(fs) > 1:
+        arrs = arrs * len(fs)
+    if any(f.p2g for f in fs):
+        raise TypeError("g2p_adjoint needs G2P functors")
+    xb = _as_list(x_bar)
+    ab = _as_list(array_bar) if array_bar is not None else [None] * len(fs)
+    if len(ab) == 1 and len(fs) > 1:
+        ab = ab * len(fs)
+    _adjoint_call(L.lib().cgx_g2p_adjoint, fs, points, num_point, spline, halo, [None] * len(fs), xb,
+                  arrs, ab, points_bar, precision, tiling, handle, stream, check_bounds)
+
+
 def last_dispatch(handle=None):
     """Kernel family of the last p2g / g2p on the handle: 'points' or 'tiled'."""
     h = handle or L.default_handle()

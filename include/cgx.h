@@ -61,6 +61,10 @@ typedef int cgx_status;
 #define CGX_SCALAR_GRADIENT_P2G 2    /* ScalarGradientP2G   :1424-1462 */
 #define CGX_VECTOR_DIVERGENCE_P2G 3  /* VectorDivergenceP2G :1473-1513 */
 #define CGX_TENSOR_DIVERGENCE_P2G 4  /* TensorDivergenceP2G :1524-1566 */
+/* No reference counterpart: TensorDivergenceP2G of the transposed tensor,
+ * grid_m += sum_n dW/dx_n * f[n][m]. It is the grid adjoint of
+ * VectorGradientG2P (cgx_g2p_adjoint). */
+#define CGX_TENSOR_DIVERGENCE_T_P2G 5
 
 /* G2P operator kinds: the functors of
  * grid/src/Cabana_Grid_Interpolation.hpp:938-1182. */
@@ -69,6 +73,10 @@ typedef int cgx_status;
 #define CGX_SCALAR_GRADIENT_G2P 2    /* ScalarGradientG2P   :1039-1079 */
 #define CGX_VECTOR_GRADIENT_G2P 3    /* VectorGradientG2P   :1090-1132 */
 #define CGX_VECTOR_DIVERGENCE_G2P 4  /* VectorDivergenceG2P :1143-1182 */
+/* No reference counterpart: VectorGradientG2P stored transposed,
+ * x[m][n] += multiplier * sum dW/dx_n * f_m. It is the point-field adjoint of
+ * TensorDivergenceP2G (cgx_p2g_adjoint). */
+#define CGX_VECTOR_GRADIENT_T_G2P 5
 
 /* Flags for cgx_p2g / cgx_g2p. */
 #define CGX_FLAG_SKIP_HALO 1u     /* do not run the halo scatter / gather step   */
@@ -188,6 +196,65 @@ cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points,
                    int64_t num_point, int spline_order, const cgx_op* ops,
                    int n_ops, int precision, const cgx_tiling* tiling,
                    unsigned flags, void* stream);
+
+/* ---- adjoints (no reference counterpart) ------------------------------ */
+
+/*
+ * One operator of an adjoint call: the forward operator (kind, multiplier)
+ * and the forward and cotangent buffers it touches. For cgx_p2g_adjoint the
+ * kind is a P2G kind; `x` is the forward input field (read for the position
+ * adjoint), `x_bar` receives dL/dx (ADDED; data NULL skips it), `array_bar`
+ * holds dL/d(forward array) (read) and `array` is unused. For cgx_g2p_adjoint
+ * the kind is a G2P kind; `x_bar` holds dL/d(forward output field) (read),
+ * `array` is the forward array (read for the position adjoint), `array_bar`
+ * receives dL/d(array) (ADDED; data NULL skips it) and `x` is unused.
+ */
+typedef struct cgx_adjoint_op {
+    int32_t kind;
+    int32_t reserved;
+    double multiplier;
+    cgx_field x;
+    cgx_field x_bar;
+    cgx_array array;
+    cgx_array array_bar;
+} cgx_adjoint_op;
+
+/*
+ * Reverse-mode derivative of cgx_p2g for the same points, order and ops.
+ * Point fields: dL/dx = multiplier * G2P of array_bar with the transposed
+ * operator (ScalarValue -> ScalarValueG2P, VectorValue -> VectorValueG2P,
+ * ScalarGradient -> VectorDivergenceG2P, VectorDivergence ->
+ * ScalarGradientG2P, TensorDivergence -> CGX_VECTOR_GRADIENT_T_G2P); it runs
+ * on the tiled kernels when `tiling` allows, as cgx_g2p does. Positions:
+ * dL/d(points) is ADDED to `points_bar` (n x 3, any cgx_field layout; NULL
+ * skips it), from the spline gradient (value operators) or Hessian
+ * (gradient and divergence operators). On periodic meshes the adjoint of
+ * the halo scatter(Sum) runs first, in place on each distinct array_bar
+ * (ghost += its owned image), unless CGX_FLAG_SKIP_HALO is set.
+ */
+cgx_status cgx_p2g_adjoint(cgx_handle h, const cgx_mesh* mesh,
+                           const cgx_field* points, int64_t num_point,
+                           int spline_order, const cgx_adjoint_op* ops,
+                           int n_ops, int precision, const cgx_tiling* tiling,
+                           const cgx_field* points_bar, unsigned flags,
+                           void* stream);
+
+/*
+ * Reverse-mode derivative of cgx_g2p. Grid: array_bar += P2G of x_bar with
+ * the transposed operator (ScalarValue -> ScalarValueP2G, VectorValue ->
+ * VectorValueP2G, ScalarGradient -> VectorDivergenceP2G, VectorGradient ->
+ * CGX_TENSOR_DIVERGENCE_T_P2G, VectorDivergence -> ScalarGradientP2G), then,
+ * on periodic meshes, the adjoint of the halo gather: every ghost of
+ * array_bar that has an owned image is added to that image and cleared
+ * (ghosts must hold no other cotangent on entry). Positions: as
+ * cgx_p2g_adjoint, using `array` as the forward array after its gather.
+ */
+cgx_status cgx_g2p_adjoint(cgx_handle h, const cgx_mesh* mesh,
+                           const cgx_field* points, int64_t num_point,
+                           int spline_order, const cgx_adjoint_op* ops,
+                           int n_ops, int precision, const cgx_tiling* tiling,
+                           const cgx_field* points_bar, unsigned flags,
+                           void* stream);
 
 /* Halo::scatter(exec, ScatterReduce::Sum(), array) and Halo::gather(exec,
  * array) for NodeHaloPattern<3> on one rank (grid/src/Cabana_Grid_HaloBase.hpp:

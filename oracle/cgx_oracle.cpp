@@ -143,6 +143,50 @@ void gradient(int order, double x0, double rdx, double* g) {
     }
 }
 
+// Second derivatives of the knot weights in the physical coordinate (no
+// reference counterpart; the reference has value and gradient only): the
+// derivative of gradient() above. Orders 2 and 3 differentiate the closed
+// forms; higher orders use d2/du2 B_n = B_{n-2}[a-2] - 2 B_{n-2}[a-1] + B_{n-2}[a].
+void hessian(int order, double x0, double rdx, double* h) {
+    const double xi = x0 - static_cast<int>(x0);
+    const double r2 = rdx * rdx;
+    switch (order) {
+        case 0:
+            h[0] = 0.0;
+            return;
+        case 1:
+            h[0] = h[1] = 0.0;
+            return;
+        case 2:  // d/dxn of (xn - 1.5), (-2 xn), (xn + 1.5)
+            h[0] = r2;
+            h[1] = -2.0 * r2;
+            h[2] = r2;
+            return;
+        case 3: {  // d/dxn of the four gradient polynomials
+            double xn = xi + 1.0;
+            h[0] = (-xn + 2.0) * r2;
+            xn -= 1.0;
+            h[1] = (3.0 * xn - 2.0) * r2;
+            xn -= 1.0;
+            h[2] = (-3.0 * xn - 2.0) * r2;
+            xn -= 1.0;
+            h[3] = (xn + 2.0) * r2;
+            return;
+        }
+        default: {
+            double b[kMaxKnot + 1];
+            de_boor(order - 2, xi, b);
+            for (int a = 0; a <= order; ++a) {
+                const double l2 = (a >= 2) ? b[a - 2] : 0.0;
+                const double l1 = (a >= 1 && a - 1 <= order - 2) ? b[a - 1] : 0.0;
+                const double l0 = (a <= order - 2) ? b[a] : 0.0;
+                h[a] = (l2 - 2.0 * l1 + l0) * r2;
+            }
+            return;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // LocalMesh<UniformMesh> (LocalMesh.hpp:180-200) and evaluateSpline
 // (Splines.hpp:1283-1342).
@@ -259,10 +303,11 @@ void p2g_point(int kind, double mult, const double* xp, const Spline3& sd, GridV
                     }
             return;
         }
-        case 4: {  // TensorDivergenceP2G (:1544-1555) -> P2G::divergence :712-747
+        case 4:    // TensorDivergenceP2G (:1544-1555) -> P2G::divergence :712-747
+        case 5: {  // the same on the transposed tensor (no reference counterpart)
             double pd[3][3];
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) pd[a][b] = mult * xp[a * 3 + b];
+                for (int b = 0; b < 3; ++b) pd[a][b] = mult * (kind == 5 ? xp[b * 3 + a] : xp[a * 3 + b]);
             for (int i = 0; i < nk; ++i)
                 for (int j = 0; j < nk; ++j)
                     for (int k = 0; k < nk; ++k) {
@@ -283,7 +328,7 @@ int p2g_comps(int kind) {
     switch (kind) {
         case 0: case 2: return 1;
         case 1: case 3: return 3;
-        case 4: return 9;
+        case 4: case 5: return 9;
     }
     return -1;
 }
@@ -291,7 +336,7 @@ int g2p_comps(int kind) {
     switch (kind) {
         case 0: case 4: return 1;
         case 1: case 2: return 3;
-        case 3: return 9;
+        case 3: case 5: return 9;
     }
     return -1;
 }
@@ -335,7 +380,8 @@ void g2p_point(int kind, double mult, double* xp, const Spline3& sd, GridView& v
             for (int d = 0; d < 3; ++d) xp[d] += mult * result[d];
             return;
         }
-        case 3: {  // VectorGradientG2P -> G2P::gradient :247-282 (result[m][n] = d_m W * f_n)
+        case 3:    // VectorGradientG2P -> G2P::gradient :247-282 (result[m][n] = d_m W * f_n)
+        case 5: {  // the same stored transposed (no reference counterpart)
             double result[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
             for (int i = 0; i < nk; ++i)
                 for (int j = 0; j < nk; ++j)
@@ -351,7 +397,7 @@ void g2p_point(int kind, double mult, double* xp, const Spline3& sd, GridView& v
                         }
                     }
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) xp[a * 3 + b] += mult * result[a][b];
+                for (int b = 0; b < 3; ++b) xp[kind == 5 ? b * 3 + a : a * 3 + b] += mult * result[a][b];
             return;
         }
         case 4: {  // VectorDivergenceG2P -> G2P::divergence :333-364
@@ -625,6 +671,69 @@ void oracle_permute(const uint64_t* permutes, int64_t begin, int64_t end, double
         for (int c = 0; c < comps; ++c) data[i * comps + c] = scratch[size_t(i - begin) * comps + c];
 }
 
+void oracle_spline_hessian(int order, double x0, double rdx, double* h) { hessian(order, x0, rdx, h); }
+
+}  // extern "C"
+
+namespace {
+
+// Node weight W_n, its gradient dW[e] and Hessian ddW[e][d] at stencil node
+// (i, j, k) of a point, from the per-dimension value / gradient / second
+// derivative tables.
+struct NodeWeights {
+    double W;
+    double dW[3];
+    double ddW[3][3];
+};
+
+NodeWeights node_weights(const Spline3& sd, const double (*h)[kMaxKnot], int i, int j, int k) {
+    const int id[3] = {i, j, k};
+    NodeWeights nw;
+    nw.W = sd.w[0][i] * sd.w[1][j] * sd.w[2][k];
+    for (int e = 0; e < 3; ++e) {
+        double t = 1.0;
+        for (int a = 0; a < 3; ++a) t *= (a == e) ? sd.g[a][id[a]] : sd.w[a][id[a]];
+        nw.dW[e] = t;
+        for (int d = 0; d < 3; ++d) {
+            double u = 1.0;
+            for (int a = 0; a < 3; ++a) {
+                if (a == e && a == d)
+                    u *= h[a][id[a]];
+                else if (a == e || a == d)
+                    u *= sd.g[a][id[a]];
+                else
+                    u *= sd.w[a][id[a]];
+            }
+            nw.ddW[e][d] = u;
+        }
+    }
+    return nw;
+}
+
+void halo_apply(const oracle_mesh& m, double* array, int dofs, bool gather_add) {
+    int64_t ext[3];
+    extents(m, ext);
+    GridView v{array, ext[0], ext[1], ext[2], dofs};
+    for (int64_t i = 0; i < ext[0]; ++i)
+        for (int64_t j = 0; j < ext[1]; ++j)
+            for (int64_t k = 0; k < ext[2]; ++k) {
+                int64_t idx[3] = {i, j, k}, own[3];
+                if (!halo_partner(m, ext, idx, own)) continue;
+                for (int c = 0; c < dofs; ++c) {
+                    if (gather_add) {
+                        v.at(i, j, k, c) += v.at(own[0], own[1], own[2], c);
+                    } else {
+                        v.at(own[0], own[1], own[2], c) += v.at(i, j, k, c);
+                        v.at(i, j, k, c) = 0.0;
+                    }
+                }
+            }
+}
+
+}  // namespace
+
+extern "C" {
+
 void oracle_stable_sort_keys(const uint64_t* keys, int64_t n, uint64_t* permutes) {
     std::vector<uint64_t> idx(n);
     std::iota(idx.begin(), idx.end(), 0);
@@ -632,4 +741,161 @@ void oracle_stable_sort_keys(const uint64_t* keys, int64_t n, uint64_t* permutes
     std::copy(idx.begin(), idx.end(), permutes);
 }
 
+
+// Reverse-mode derivative of oracle_p2g (no reference counterpart): each
+// forward operator written out term by term, differentiated by hand with
+// respect to its point field and to the point position. array_bar holds
+// dL/d(array); on periodic meshes the adjoint of the halo scatter(Sum)
+// (ghost += owned image) is applied to it first, in place.
+int oracle_p2g_adjoint(const oracle_mesh* mesh, const double* points, int64_t num_point, int order,
+                       const oracle_adjoint_op* ops, int n_ops, double* points_bar) {
+    int64_t ext[3];
+    extents(*mesh, ext);
+    for (int o = 0; o < n_ops; ++o) {
+        bool seen = false;
+        for (int q = 0; q < o; ++q) seen |= (ops[q].array_bar == ops[o].array_bar);
+        if (!seen) halo_apply(*mesh, ops[o].array_bar, ops[o].dofs, true);
+    }
+    int skipped = 0;
+    for (int64_t p = 0; p < num_point; ++p) {
+        Spline3 sd;
+        evaluate(*mesh, order, points + 3 * p, sd);
+        if (!stencil_in_range(sd, ext)) { ++skipped; continue; }
+        double h[3][kMaxKnot];
+        for (int d = 0; d < 3; ++d) hessian(order, sd.x[d], 1.0 / sd.dx[d], h[d]);
+        double pos[3] = {0.0, 0.0, 0.0};
+        for (int o = 0; o < n_ops; ++o) {
+            const oracle_adjoint_op& op = ops[o];
+            const int nc = p2g_comps(op.kind);
+            const double* x = op.x ? op.x + p * nc : nullptr;
+            double* xb = op.x_bar ? op.x_bar + p * nc : nullptr;
+            GridView v{op.array_bar, ext[0], ext[1], ext[2], op.dofs};
+            const double m = op.multiplier;
+            for (int i = 0; i < sd.nk; ++i)
+                for (int j = 0; j < sd.nk; ++j)
+                    for (int k = 0; k < sd.nk; ++k) {
+                        const NodeWeights nw = node_weights(sd, h, i, j, k);
+                        double A[3];
+                        for (int c = 0; c < 3; ++c)
+                            A[c] = c < op.dofs ? v.at(sd.s[0][i], sd.s[1][j], sd.s[2][k], c) : 0.0;
+                        for (int e = 0; e < 3; ++e) {
+                            double t = 0.0;
+                            switch (op.kind) {
+                                case 0: if (x) t = x[0] * A[0] * nw.dW[e]; break;
+                                case 1: if (x) for (int d = 0; d < 3; ++d) t += x[d] * A[d] * nw.dW[e]; break;
+                                case 2: if (x) for (int d = 0; d < 3; ++d) t += x[0] * A[d] * nw.ddW[e][d]; break;
+                                case 3: if (x) for (int d = 0; d < 3; ++d) t += A[0] * x[d] * nw.ddW[e][d]; break;
+                                case 4:
+                                    if (x) for (int a = 0; a < 3; ++a)
+                                        for (int d = 0; d < 3; ++d) t += A[a] * x[a * 3 + d] * nw.ddW[e][d];
+                                    break;
+                                case 5:
+                                    if (x) for (int a = 0; a < 3; ++a)
+                                        for (int d = 0; d < 3; ++d) t += A[a] * x[d * 3 + a] * nw.ddW[e][d];
+                                    break;
+                            }
+                            pos[e] += m * t;
+                        }
+                        if (!xb) continue;
+                        switch (op.kind) {
+                            case 0: xb[0] += m * A[0] * nw.W; break;
+                            case 1: for (int d = 0; d < 3; ++d) xb[d] += m * A[d] * nw.W; break;
+                            case 2: for (int d = 0; d < 3; ++d) xb[0] += m * A[d] * nw.dW[d]; break;
+                            case 3: for (int d = 0; d < 3; ++d) xb[d] += m * A[0] * nw.dW[d]; break;
+                            case 4:
+                                for (int a = 0; a < 3; ++a)
+                                    for (int d = 0; d < 3; ++d) xb[a * 3 + d] += m * A[a] * nw.dW[d];
+                                break;
+                            case 5:
+                                for (int a = 0; a < 3; ++a)
+                                    for (int d = 0; d < 3; ++d) xb[d * 3 + a] += m * A[a] * nw.dW[d];
+                                break;
+                        }
+                    }
+        }
+        if (points_bar)
+            for (int e = 0; e < 3; ++e) points_bar[p * 3 + e] += pos[e];
+    }
+    return skipped;
+}
+
+// Reverse-mode derivative of oracle_g2p (no reference counterpart). x_bar
+// holds dL/d(forward output field); array is the forward array as the
+// forward read it (after its halo gather). array_bar (may be NULL) receives
+// dL/d(array); on periodic meshes the adjoint of the halo gather (owned image
+// += ghost, ghost = 0) is applied to it afterwards.
+int oracle_g2p_adjoint(const oracle_mesh* mesh, const double* points, int64_t num_point, int order,
+                       const oracle_adjoint_op* ops, int n_ops, double* points_bar) {
+    int64_t ext[3];
+    extents(*mesh, ext);
+    int skipped = 0;
+    for (int64_t p = 0; p < num_point; ++p) {
+        Spline3 sd;
+        evaluate(*mesh, order, points + 3 * p, sd);
+        if (!stencil_in_range(sd, ext)) { ++skipped; continue; }
+        double h[3][kMaxKnot];
+        for (int d = 0; d < 3; ++d) hessian(order, sd.x[d], 1.0 / sd.dx[d], h[d]);
+        double pos[3] = {0.0, 0.0, 0.0};
+        for (int o = 0; o < n_ops; ++o) {
+            const oracle_adjoint_op& op = ops[o];
+            const int nc = g2p_comps(op.kind);
+            const double* sb = op.x_bar + p * nc;
+            GridView va{op.array, ext[0], ext[1], ext[2], op.dofs};
+            GridView vb{op.array_bar, ext[0], ext[1], ext[2], op.dofs};
+            const double m = op.multiplier;
+            for (int i = 0; i < sd.nk; ++i)
+                for (int j = 0; j < sd.nk; ++j)
+                    for (int k = 0; k < sd.nk; ++k) {
+                        const int ni = sd.s[0][i], nj = sd.s[1][j], nkk = sd.s[2][k];
+                        const NodeWeights nw = node_weights(sd, h, i, j, k);
+                        if (op.array) {
+                            double A[3];
+                            for (int c = 0; c < 3; ++c) A[c] = c < op.dofs ? va.at(ni, nj, nkk, c) : 0.0;
+                            for (int e = 0; e < 3; ++e) {
+                                double t = 0.0;
+                                switch (op.kind) {
+                                    case 0: t = sb[0] * A[0] * nw.dW[e]; break;
+                                    case 1: for (int d = 0; d < 3; ++d) t += sb[d] * A[d] * nw.dW[e]; break;
+                                    case 2: for (int d = 0; d < 3; ++d) t += sb[d] * A[0] * nw.ddW[e][d]; break;
+                                    case 3:
+                                        for (int a = 0; a < 3; ++a)
+                                            for (int b = 0; b < 3; ++b) t += sb[a * 3 + b] * A[b] * nw.ddW[e][a];
+                                        break;
+                                    case 4: for (int d = 0; d < 3; ++d) t += sb[0] * A[d] * nw.ddW[e][d]; break;
+                                    case 5:
+                                        for (int a = 0; a < 3; ++a)
+                                            for (int b = 0; b < 3; ++b) t += sb[b * 3 + a] * A[b] * nw.ddW[e][a];
+                                        break;
+                                }
+                                pos[e] += m * t;
+                            }
+                        }
+                        if (!op.array_bar) continue;
+                        switch (op.kind) {
+                            case 0: vb.at(ni, nj, nkk, 0) += m * sb[0] * nw.W; break;
+                            case 1: for (int d = 0; d < 3; ++d) vb.at(ni, nj, nkk, d) += m * sb[d] * nw.W; break;
+                            case 2: for (int d = 0; d < 3; ++d) vb.at(ni, nj, nkk, 0) += m * sb[d] * nw.dW[d]; break;
+                            case 3:
+                                for (int a = 0; a < 3; ++a)
+                                    for (int b = 0; b < 3; ++b) vb.at(ni, nj, nkk, b) += m * sb[a * 3 + b] * nw.dW[a];
+                                break;
+                            case 4: for (int d = 0; d < 3; ++d) vb.at(ni, nj, nkk, d) += m * sb[0] * nw.dW[d]; break;
+                            case 5:
+                                for (int a = 0; a < 3; ++a)
+                                    for (int b = 0; b < 3; ++b) vb.at(ni, nj, nkk, b) += m * sb[b * 3 + a] * nw.dW[a];
+                                break;
+                        }
+                    }
+        }
+        if (points_bar)
+            for (int e = 0; e < 3; ++e) points_bar[p * 3 + e] += pos[e];
+    }
+    for (int o = 0; o < n_ops; ++o) {
+        if (!ops[o].array_bar) continue;
+        bool seen = false;
+        for (int q = 0; q < o; ++q) seen |= (ops[q].array_bar == ops[o].array_bar);
+        if (!seen) halo_apply(*mesh, ops[o].array_bar, ops[o].dofs, false);
+    }
+    return skipped;
+}
 }  // extern "C"

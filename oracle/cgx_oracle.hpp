@@ -99,6 +99,36 @@ void oracle_bin_by_key(const int32_t* keys, int64_t begin, int64_t end,
 void oracle_permute(const uint64_t* permutes, int64_t begin, int64_t end,
                     double* data, int comps);
 
+// Second derivatives of the knot weights in the physical coordinate.
+void oracle_spline_hessian(int order, double x0, double rdx, double* h);
+
+// One operator of an adjoint call: dense (n, comps) point arrays and dense
+// (i, j, k, dof) grid arrays. P2G adjoint: x = forward input (read; NULL
+// skips the position term), x_bar = dL/dx (added; may be NULL), array_bar =
+// dL/d(array) (read; halo-adjusted in place). G2P adjoint: x_bar =
+// dL/d(output) (read), array = forward array (read; NULL skips the position
+// term), array_bar = dL/d(array) (added; may be NULL).
+typedef struct oracle_adjoint_op {
+    int32_t kind;
+    int32_t dofs;
+    double multiplier;
+    double* x;
+    double* x_bar;
+    double* array;
+    double* array_bar;
+} oracle_adjoint_op;
+
+// Reverse-mode derivatives of oracle_p2g / oracle_g2p; points_bar (n, 3)
+// receives dL/d(position), added (may be NULL). Return the skipped count.
+int oracle_p2g_adjoint(const oracle_mesh* mesh, const double* points,
+                       int64_t num_point, int order,
+                       const oracle_adjoint_op* ops, int n_ops,
+                       double* points_bar);
+int oracle_g2p_adjoint(const oracle_mesh* mesh, const double* points,
+                       int64_t num_point, int order,
+                       const oracle_adjoint_op* ops, int n_ops,
+                       double* points_bar);
+
 // Stable key sort used to order particles tile by tile; returns the gather
 // permutation.
 void oracle_stable_sort_keys(const uint64_t* keys, int64_t n,

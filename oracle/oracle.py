@@ -18,10 +18,11 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 
-P2G_COMPS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 9}
-P2G_DOFS = {0: 1, 1: 3, 2: 3, 3: 1, 4: 3}
-G2P_COMPS = {0: 1, 1: 3, 2: 3, 3: 9, 4: 1}
-G2P_DOFS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 3}
+# kind 5 is the transposed tensor form (no reference counterpart) used by the adjoints
+P2G_COMPS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 9, 5: 9}
+P2G_DOFS = {0: 1, 1: 3, 2: 3, 3: 1, 4: 3, 5: 3}
+G2P_COMPS = {0: 1, 1: 3, 2: 3, 3: 9, 4: 1, 5: 9}
+G2P_DOFS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 3, 5: 3}
 
 
 class OracleMesh(ctypes.Structure):
@@ -42,6 +43,18 @@ class OracleOp(ctypes.Structure):
         ("multiplier", ctypes.c_double),
         ("x", ctypes.POINTER(ctypes.c_double)),
         ("array", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+class OracleAdjointOp(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("dofs", ctypes.c_int32),
+        ("multiplier", ctypes.c_double),
+        ("x", ctypes.POINTER(ctypes.c_double)),
+        ("x_bar", ctypes.POINTER(ctypes.c_double)),
+        ("array", ctypes.POINTER(ctypes.c_double)),
+        ("array_bar", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -67,6 +80,10 @@ def lib():
         _lib.oracle_p2g.argtypes = [ctypes.POINTER(OracleMesh), dp, ctypes.c_int64, ctypes.c_int,
                                     ctypes.POINTER(OracleOp), ctypes.c_int, ctypes.c_int]
         _lib.oracle_g2p.argtypes = _lib.oracle_p2g.argtypes
+        _lib.oracle_spline_hessian.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, dp]
+        _lib.oracle_p2g_adjoint.argtypes = [ctypes.POINTER(OracleMesh), dp, ctypes.c_int64, ctypes.c_int,
+                                            ctypes.POINTER(OracleAdjointOp), ctypes.c_int, dp]
+        _lib.oracle_g2p_adjoint.argtypes = _lib.oracle_p2g_adjoint.argtypes
     return _lib
 
 
@@ -113,6 +130,12 @@ def spline_value(order, x0):
 def spline_gradient(order, x0, rdx):
     v = np.zeros(num_knot(order))
     lib().oracle_spline_gradient(order, x0, rdx, _dp(v))
+    return v
+
+
+def spline_hessian(order, x0, rdx):
+    v = np.zeros(num_knot(order))
+    lib().oracle_spline_hessian(order, x0, rdx, _dp(v))
     return v
 
 
@@ -171,6 +194,40 @@ def g2p(mesh, points, order, ops, nthreads=1):
     n = points.shape[0]
     arr, _keep = _ops(ops, n, G2P_COMPS)
     return lib().oracle_g2p(ctypes.byref(mesh), _dp(points), n, order, arr, len(ops), nthreads)
+
+
+def _adjoint(fn, mesh, points, order, ops, points_bar):
+    points = np.ascontiguousarray(points, np.float64)
+    n = points.shape[0]
+    arr = (OracleAdjointOp * max(1, len(ops)))()
+    null = ctypes.POINTER(ctypes.c_double)()
+    for i, op in enumerate(ops):
+        for key in ("x", "x_bar", "array", "array_bar"):
+            a = op.get(key)
+            assert a is None or (a.dtype == np.float64 and a.flags.c_contiguous), key
+        grid = op.get("array_bar") if op.get("array_bar") is not None else op.get("array")
+        arr[i].kind = op["kind"]
+        arr[i].dofs = grid.shape[3]
+        arr[i].multiplier = float(op["mult"])
+        for key in ("x", "x_bar", "array", "array_bar"):
+            setattr(arr[i], key, _dp(op[key]) if op.get(key) is not None else null)
+    pb = _dp(points_bar) if points_bar is not None else null
+    return fn(ctypes.byref(mesh), _dp(points), n, order, arr, len(ops), pb)
+
+
+def p2g_adjoint(mesh, points, order, ops, points_bar=None):
+    """Reverse mode of p2g. ops: dicts with kind, mult, x (forward input or
+    None), x_bar (dL/dx, added, or None), array_bar (dL/d array, read; its
+    ghosts are halo-adjusted in place on periodic meshes). points_bar (n, 3)
+    receives dL/d(position), added."""
+    return _adjoint(lib().oracle_p2g_adjoint, mesh, points, order, ops, points_bar)
+
+
+def g2p_adjoint(mesh, points, order, ops, points_bar=None):
+    """Reverse mode of g2p. ops: dicts with kind, mult, x_bar (dL/d output,
+    read), array (forward array or None), array_bar (dL/d array, added, or
+    None). points_bar (n, 3) receives dL/d(position), added."""
+    return _adjoint(lib().oracle_g2p_adjoint, mesh, points, order, ops, points_bar)
 
 
 def halo_scatter_sum(mesh, array):

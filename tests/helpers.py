@@ -5,10 +5,11 @@ import numpy as np
 
 from cabana_gb300 import mesh as M
 
-P2G_COMPS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 9}
-P2G_DOFS = {0: 1, 1: 3, 2: 3, 3: 1, 4: 3}
-G2P_COMPS = {0: 1, 1: 3, 2: 3, 3: 9, 4: 1}
-G2P_DOFS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 3}
+# kind 5: the transposed tensor operators (no reference counterpart; adjoints)
+P2G_COMPS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 9, 5: 9}
+P2G_DOFS = {0: 1, 1: 3, 2: 3, 3: 1, 4: 3, 5: 3}
+G2P_COMPS = {0: 1, 1: 3, 2: 3, 3: 9, 4: 1, 5: 9}
+G2P_DOFS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 3, 5: 3}
 P2G_NAMES = ["ScalarValueP2G", "VectorValueP2G", "ScalarGradientP2G", "VectorDivergenceP2G", "TensorDivergenceP2G"]
 G2P_NAMES = ["ScalarValueG2P", "VectorValueG2P", "ScalarGradientG2P", "VectorGradientG2P", "VectorDivergenceG2P"]
 

@@ -46,6 +46,8 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu\\n", sizeof(cgx_mesh), sizeof(cgx_field), sizeof(cgx_array), sizeof(cgx_op), sizeof(cgx_tiling));
   printf("%zu %zu %zu %zu\\n", offsetof(cgx_mesh, owned_cells), offsetof(cgx_mesh, entity), offsetof(cgx_op, x), offsetof(cgx_op, array));
   printf("%zu %zu\\n", offsetof(cgx_field, soa_stride), offsetof(cgx_tiling, tile_offsets));
+  printf("%zu %zu %zu %zu\\n", sizeof(cgx_adjoint_op), offsetof(cgx_adjoint_op, x_bar), offsetof(cgx_adjoint_op, array),
+         offsetof(cgx_adjoint_op, array_bar));
   return 0;
 }
 """)
@@ -55,7 +57,9 @@ int main(void) {
     got = list(map(int, out))
     want = [ctypes.sizeof(L.CgxMesh), ctypes.sizeof(L.CgxField), ctypes.sizeof(L.CgxArray), ctypes.sizeof(L.CgxOp),
             ctypes.sizeof(L.CgxTiling), L.CgxMesh.owned_cells.offset, L.CgxMesh.entity.offset, L.CgxOp.x.offset,
-            L.CgxOp.array.offset, L.CgxField.soa_stride.offset, L.CgxTiling.tile_offsets.offset]
+            L.CgxOp.array.offset, L.CgxField.soa_stride.offset, L.CgxTiling.tile_offsets.offset,
+            ctypes.sizeof(L.CgxAdjointOp), L.CgxAdjointOp.x_bar.offset, L.CgxAdjointOp.array.offset,
+            L.CgxAdjointOp.array_bar.offset]
     assert got == want
 
 
@@ -84,6 +88,10 @@ def test_argument_checks_fail_loudly(lib):
     ops = (L.CgxOp * 1)()
     # NULL handle
     st = lib.cgx_p2g(None, ctypes.byref(mesh), ctypes.byref(pts), 1, 1, ops, 1, 0, None, 0, None)
+    assert st == L.CGX_ERR_INVALID_ARG
+    assert b"handle" in lib.cgx_last_error()
+    aops = (L.CgxAdjointOp * 1)()
+    st = lib.cgx_p2g_adjoint(None, ctypes.byref(mesh), ctypes.byref(pts), 1, 1, aops, 1, 0, None, None, 0, None)
     assert st == L.CGX_ERR_INVALID_ARG
     assert b"handle" in lib.cgx_last_error()
     bad = L.CgxMesh()
