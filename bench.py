@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 512-instance ensemble leg")
+    ap.add_argument("--batch-instances", type=int, default=512)
+    ap.add_argument("--batch-seed", type=int, default=5)
     return ap.parse_args()
 
 
@@ -195,6 +198,125 @@ class Transfer:
     def g2p(self):
         self.G.g2p(self.mom_g, self.halo, self.pos, self.n, self.G.Spline(2), self.g2p_f, precision=self.precision,
                    tiling=self.tiling)
+
+
+def batched_leg(args, dev):
+    """Ensemble of independent meshes: 512 instances, cube side ~U{16..96}
+    cells, particle counts log-uniform in [1e3, 1e6], each instance uniform or
+    1-8 Gaussian clumps (sigma = side / 10). Quadratic spline, FP32 form: P2G
+    mass + momentum, G2P velocity + velocity gradient from the momentum array.
+    Compares per-instance calls (one work list and one launch per instance and
+    direction) with one autotuned batched plan per direction replayed from a
+    CUDA graph."""
+    import torch
+
+    from cabana_gb300 import grid as G
+    from cabana_gb300 import mesh as M
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.batch_seed)
+    rng = torch.Generator()
+    rng.manual_seed(args.batch_seed)
+    inst = []
+    total = 0
+    sides = [int(torch.randint(16, 97, (1,), generator=rng)) for _ in range(args.batch_instances)]
+    # every instance's grid arrays live in one pooled buffer: one fill zeroes them all
+    pool = torch.zeros(sum(4 * (s + 3) ** 3 for s in sides), device=dev)
+    at = 0
+    for side in sides:
+        n = int(torch.exp(torch.empty(1).uniform_(float(torch.log(torch.tensor(1e3))),
+                                                  float(torch.log(torch.tensor(1e6))), generator=rng)))
+        clumps = int(torch.randint(0, 9, (1,), generator=rng))
+        lg, mp = M.simple_mesh(side, 1.0, (0.0, 0.0, 0.0), 1)
+        L = float(side)
+        if clumps == 0:
+            pos = torch.rand((n, 3), generator=g, device=dev, dtype=torch.float64) * L
+        else:
+            sig = side / 10.0
+            centres = torch.rand((clumps, 3), generator=g, device=dev, dtype=torch.float64) * L
+            which = torch.randint(0, clumps, (n,), generator=g, device=dev)
+            pos = centres[which] + torch.randn((n, 3), generator=g, device=dev, dtype=torch.float64) * sig
+            for _ in range(64):
+                bad = ((pos < 0) | (pos >= L)).any(dim=1)
+                nb = int(bad.sum())
+                if nb == 0:
+                    break
+                idx = bad.nonzero().squeeze(1)
+                pos[idx] = centres[which[idx]] + torch.randn((nb, 3), generator=g, device=dev,
+                                                             dtype=torch.float64) * sig
+        mass = torch.rand((n,), generator=g, device=dev) + 0.5
+        vel = torch.randn((n, 3), generator=g, device=dev)
+        til = G.Tiling(mp, 2, (8, 8, 8), device=dev)
+        perm = til.sort(pos, n)
+        pos, mass, vel = pos[perm].contiguous(), mass[perm].contiguous(), vel[perm].contiguous()
+        e = (side + 3,) * 3
+        nn = e[0] * e[1] * e[2]
+        mg = G.createArray("m", G.createArrayLayout(lg, 1, G.Node), torch.float32,
+                           data=pool[at:at + nn].view(e + (1,)))
+        pg = G.createArray("p", G.createArrayLayout(lg, 3, G.Node), torch.float32,
+                           data=pool[at + nn:at + 4 * nn].view(e + (3,)))
+        at += 4 * nn
+        inst.append(dict(pos=pos, n=n, til=til, mass=mass, mom=(mass[:, None] * vel).contiguous(), mg=mg, pg=pg,
+                         v=torch.zeros((n, 3), device=dev), vg=torch.zeros((n, 3, 3), device=dev)))
+        total += n
+
+    def zero():
+        pool.zero_()
+
+    def per_instance():
+        zero()
+        for b in inst:
+            G.p2g([G.createScalarValueP2G(b["mass"], 1.0), G.createVectorValueP2G(b["mom"], 1.0)], b["pos"], b["n"],
+                  G.Spline(2), None, [b["mg"], b["pg"]], precision=G.FP32_COMPENSATED, tiling=b["til"])
+        for b in inst:
+            G.g2p(b["pg"], None, b["pos"], b["n"], G.Spline(2),
+                  [G.createVectorValueG2P(b["v"], 1.0), G.createVectorGradientG2P(b["vg"], 1.0)],
+                  precision=G.FP32_COMPENSATED, tiling=b["til"])
+
+    pp = G.BatchPlan([G.createScalarValueP2G(None, 1.0), G.createVectorValueP2G(None, 1.0)],
+                     [G.BatchInstance(b["pos"], b["n"], b["til"], [b["mass"], b["mom"]], [b["mg"], b["pg"]])
+                      for b in inst], G.Spline(2), p2g=True)
+    gp = G.BatchPlan([G.createVectorValueG2P(None, 1.0), G.createVectorGradientG2P(None, 1.0)],
+                     [G.BatchInstance(b["pos"], b["n"], b["til"], [b["v"], b["vg"]], [b["pg"], b["pg"]])
+                      for b in inst], G.Spline(2), p2g=False)
+    t0 = time.perf_counter()
+    pp.autotune()
+    gp.autotune()
+    tune_s = time.perf_counter() - t0
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(graph, stream=s):
+            zero()
+            pp.execute(stream=s, halo=False)
+            gp.execute(stream=s, halo=False)
+
+    def timed(fn, reps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    per_ms = timed(per_instance, 3)
+    batch_ms = timed(graph.replay, 10)
+    launches_per = len(inst) * 2 * 6  # per call: work-list build (5 kernels) + 1 tiled kernel
+    return {"workload": f"{len(inst)} instances, side U{{16..96}}, particles log-uniform [1e3, 1e6], uniform or "
+                        f"1-8 clumps (sigma side/10), quadratic, P2G mass+momentum, G2P velocity+gradient",
+            "particles": total, "seed": args.batch_seed,
+            "per_instance": {"ms": per_ms, "particles_per_s": total / (per_ms / 1e3), "launches": launches_per},
+            "batched_graph": {"ms": batch_ms, "particles_per_s": total / (batch_ms / 1e3),
+                              "launches": 2 * 6,  # per direction: work list (5 kernels) + 1 tiled kernel
+                              "p2g_config": dict(zip(("item_particles", "ctas_per_sm"), pp.config())),
+                              "g2p_config": dict(zip(("item_particles", "ctas_per_sm"), gp.config())),
+                              "autotune_s": tune_s},
+            "speedup": per_ms / batch_ms}
 
 
 def time_steps(tr, steps, warmup, barrier):
@@ -463,6 +585,11 @@ def run_ours(args):
                        "permute of all particle fields, zero grids, P2G + G2P, D2H of velocity and velocity gradient"}
         del h_in, h_out
 
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = batched_leg(args, dev)
+        torch.cuda.empty_cache()
+
     cpu = None
     if sample is not None:
         times, threads = cpu_baseline(args, *sample, nsteps=1)
@@ -486,7 +613,7 @@ def run_ours(args):
                                   "frac": step_bytes / (ms_per_step / 1000.0) / 1e9 / peak},
                 "kernels_ms": {"p2g": p2g_avg, "g2p": g2p_avg},
                 "cpu_baseline": cpu, "e2e": e2e, "plain_fp64": plain, "errors": errors,
-                "occupancy": occ, "binning_s": bin_s, "gpu_launches": None, "clocks": clk}
+                "occupancy": occ, "binning_s": bin_s, "batched": batched, "gpu_launches": None, "clocks": clk}
         line["gpu_launches"] = launches_per_step() * args.steps
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -41,6 +41,8 @@ EXPORTS = (
     "cgx_p2g", "cgx_g2p", "cgx_p2g_adjoint", "cgx_g2p_adjoint", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
     "cgx_cartesian_num_bins", "cgx_linked_cell_build", "cgx_bin_by_key", "cgx_bin_by_key_static", "cgx_permute",
     "cgx_tiling_init", "cgx_tiling_num_offsets", "cgx_sort_tiles",
+    "cgx_batch_plan_create", "cgx_batch_plan_destroy", "cgx_batch_execute", "cgx_batch_autotune",
+    "cgx_batch_get_config", "cgx_batch_set_config",
 )
 
 
@@ -105,6 +107,20 @@ class CgxTiling(ctypes.Structure):
     ]
 
 
+CGX_BATCH_MAX_OPS = 8
+
+
+class CgxInstance(ctypes.Structure):
+    _fields_ = [
+        ("mesh", CgxMesh),
+        ("points", CgxField),
+        ("num_point", ctypes.c_int64),
+        ("tiling", CgxTiling),
+        ("x", CgxField * CGX_BATCH_MAX_OPS),
+        ("array", CgxArray * CGX_BATCH_MAX_OPS),
+    ]
+
+
 class CgxError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"cgx error {code}: {msg}")
@@ -138,6 +154,13 @@ def lib():
            P(CgxTiling), P(CgxField), ctypes.c_uint, vp]
     L.cgx_p2g_adjoint.argtypes = adj
     L.cgx_g2p_adjoint.argtypes = adj
+    L.cgx_batch_plan_create.argtypes = [vp, P(CgxInstance), ctypes.c_int, ctypes.c_int, P(CgxOp), ctypes.c_int,
+                                        ctypes.c_int, P(vp)]
+    L.cgx_batch_plan_destroy.argtypes = [vp]
+    L.cgx_batch_execute.argtypes = [vp, ctypes.c_uint, vp]
+    L.cgx_batch_autotune.argtypes = [vp, vp, P(ctypes.c_double)]
+    L.cgx_batch_get_config.argtypes = [vp, P(ctypes.c_int64), P(ctypes.c_int)]
+    L.cgx_batch_set_config.argtypes = [vp, ctypes.c_int64, ctypes.c_int]
     L.cgx_halo_scatter_sum.argtypes = [P(CgxMesh), P(CgxArray), vp]
     L.cgx_halo_gather.argtypes = [P(CgxMesh), P(CgxArray), vp]
     L.cgx_array_assign.argtypes = [P(CgxMesh), P(CgxArray), ctypes.c_double, vp]

@@ -3,6 +3,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "cgx_kernels.cuh"
 
@@ -332,6 +333,74 @@ cgx_status build_work(cgx_context* h, const cgx_tiling& t, int64_t num_point, cu
     return CGX_OK;
 }
 
+// The operator structure of a tiled launch (shared by every instance of a
+// batched launch): distinct-array slots, box layout in shared memory, p2g
+// channel plan. Returns false when the tiled kernels cannot take it (too
+// many channel groups, or node boxes plus staging beyond shared memory).
+bool setup_tiled(TiledParams& prm, const cgx_op* ops, int n_ops, int spline_order, bool p2g) {
+    std::memset(&prm, 0, sizeof(prm));
+    prm.n_ops = n_ops;
+    const int nk = spline_order + 1;
+    for (int d = 0; d < 3; ++d) {
+        prm.tile[d] = kTiledTile;
+        prm.box[d] = kTiledTile + nk - 1;
+    }
+    prm.box_nodes = prm.box[0] * prm.box[1] * prm.box[2];
+    int n_arrays = 0;
+    int offset = 0;
+    for (int o = 0; o < n_ops; ++o) {
+        int slot = -1;
+        for (int a = 0; a < n_arrays; ++a)
+            if (prm.arrays[a].a.data == ops[o].array.data) slot = a;
+        if (slot < 0) {
+            slot = n_arrays++;
+            prm.arrays[slot].a.data = reinterpret_cast<char*>(ops[o].array.data);
+            prm.arrays[slot].a.dtype = ops[o].array.dtype;
+            prm.arrays[slot].a.dofs = ops[o].array.dofs;
+            prm.arrays[slot].smem_offset = offset;
+            offset += prm.box_nodes * ops[o].array.dofs * (p2g ? 2 : 1);
+        }
+        prm.ops[o].kind = ops[o].kind;
+        prm.ops[o].slot = slot;
+        prm.ops[o].mult = ops[o].multiplier;
+        prm.ops[o].mult_f = float(ops[o].multiplier);
+    }
+    prm.n_arrays = n_arrays;
+    prm.smem_floats = offset;
+    bool ok = true;
+    if (p2g && !plan_channels(prm, ops, n_ops, spline_order)) ok = false;  // too many channel groups
+    // node boxes plus per-item staging must fit in one SM's shared memory
+    if (p2g) {
+        if (p2g_tiled_smem(prm, size_t(offset) * sizeof(float)) > 210 * 1024) ok = false;  // + ~9 KB static tables
+    } else {
+        // g2p_tiled_smem also refuses double point fields
+        for (int o = 0; o < n_ops; ++o) prm.ops[o].x.dtype = ops[o].x.dtype;
+        for (int a = 0; a < n_arrays; ++a)
+            if (g2p_tiled_smem(prm, a) > 220 * 1024) ok = false;
+    }
+    return ok;
+}
+
+// The mesh and buffers of one instance, with the slots of `prm`.
+void fill_geom(TiledGeom& g, const TiledParams& prm, const cgx_mesh& mesh, const cgx_field& points, const cgx_op* ops,
+               int n_ops, const cgx_tiling& tiling, int spline_order) {
+    std::memset(&g, 0, sizeof(g));
+    g.mesh = to_dmesh(mesh);
+    const int shift_even = (spline_order % 2 == 0) ? 1 : 0;
+    for (int d = 0; d < 3; ++d) {
+        g.c0[d] = -g.mesh.low[d] * g.mesh.rdx[d] + 0.5 * shift_even;
+        g.num_tiles[d] = tiling.num_tiles[d];
+    }
+    g.points = to_dfield(points);
+    for (int o = 0; o < n_ops; ++o) {
+        g.x[o] = to_dfield(ops[o].x);
+        DArray& a = g.arr[prm.ops[o].slot];
+        a.data = reinterpret_cast<char*>(ops[o].array.data);
+        a.dtype = ops[o].array.dtype;
+        a.dofs = ops[o].array.dofs;
+    }
+}
+
 cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point,
                        int spline_order, const cgx_op* ops, int n_ops, int precision, const cgx_tiling* tiling,
                        unsigned flags, void* stream, bool p2g) {
@@ -365,52 +434,11 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
                  tiling->tile[0] == kTiledTile && tiling->tile[1] == kTiledTile && tiling->tile[2] == kTiledTile;
     if (tiled) {
         TiledParams prm;
-        std::memset(&prm, 0, sizeof(prm));
-        prm.mesh = dm;
-        prm.points = to_dfield(*points);
+        tiled = setup_tiled(prm, ops, n_ops, spline_order, p2g);
+        fill_geom(prm.geom, prm, *mesh, *points, ops, n_ops, *tiling, spline_order);
         prm.num_point = num_point;
-        prm.n_ops = n_ops;
-        const int nk = spline_order + 1;
-        for (int d = 0; d < 3; ++d) {
-            prm.tile[d] = tiling->tile[d];
-            prm.num_tiles[d] = tiling->num_tiles[d];
-            prm.box[d] = tiling->tile[d] + nk - 1;
-        }
-        prm.box_nodes = prm.box[0] * prm.box[1] * prm.box[2];
-        int n_arrays = 0;
-        int offset = 0;
-        for (int o = 0; o < n_ops; ++o) {
-            int slot = -1;
-            for (int a = 0; a < n_arrays; ++a)
-                if (prm.arrays[a].a.data == ops[o].array.data) slot = a;
-            if (slot < 0) {
-                slot = n_arrays++;
-                prm.arrays[slot].a.data = reinterpret_cast<char*>(ops[o].array.data);
-                prm.arrays[slot].a.dtype = ops[o].array.dtype;
-                prm.arrays[slot].a.dofs = ops[o].array.dofs;
-                prm.arrays[slot].smem_offset = offset;
-                offset += prm.box_nodes * ops[o].array.dofs * (p2g ? 2 : 1);
-            }
-            prm.ops[o].kind = ops[o].kind;
-            prm.ops[o].slot = slot;
-            prm.ops[o].mult = ops[o].multiplier;
-            prm.ops[o].mult_f = float(ops[o].multiplier);
-            prm.ops[o].x = to_dfield(ops[o].x);
-            prm.ops[o].a = prm.arrays[slot].a;
-        }
-        prm.n_arrays = n_arrays;
-        prm.smem_floats = offset;
-        const int shift_even = (spline_order % 2 == 0) ? 1 : 0;
-        for (int d = 0; d < 3; ++d) prm.c0[d] = -dm.low[d] * dm.rdx[d] + 0.5 * shift_even;
-        if (p2g && !plan_channels(prm, ops, n_ops, spline_order)) tiled = false;  // too many channel groups
-        const size_t smem = size_t(offset) * sizeof(float);
-        // node boxes plus per-item staging must fit in one SM's shared memory
-        if (p2g) {
-            if (p2g_tiled_smem(prm, smem) > 210 * 1024) tiled = false;  // + ~9 KB static run table
-        } else {
-            for (int a = 0; a < n_arrays; ++a)
-                if (g2p_tiled_smem(prm, a) > 220 * 1024) tiled = false;
-        }
+        const int n_arrays = prm.n_arrays;
+        const size_t smem = size_t(prm.smem_floats) * sizeof(float);
         if (tiled) {
             s = build_work(h, *tiling, num_point, st);
             if (s) return s;
@@ -917,6 +945,300 @@ cgx_status cgx_sort_tiles(cgx_handle h, const cgx_mesh* mesh, const cgx_field* p
         CGX_CUDA(radix_sort_pairs(keys, num_point, key_bits_for(nt * cpt), permutes, nullptr, 0, scratch,
                                   radix_sort_scratch_bytes(num_point), h->sms, st));
     return CGX_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched launches: many independent meshes, one work list, one persistent
+// kernel per direction (per distinct array for g2p).
+// ---------------------------------------------------------------------------
+struct cgx_batch {
+    cgx_context* h = nullptr;
+    bool p2g = true;
+    int order = 2;
+    int n_inst = 0;
+    TiledParams prm;                   // operator structure; instances -> geoms
+    std::vector<cgx_mesh> meshes;      // for the halo step
+    std::vector<cgx_array> arrays;     // n_inst x n_arrays distinct arrays
+    bool any_periodic = false;
+    int64_t total_tiles = 0;
+    int64_t total_points = 0;
+    TiledGeom* geoms = nullptr;        // device
+    const int64_t** offs = nullptr;    // device: per-instance tile offsets
+    int64_t* tile_base = nullptr;      // device: n_inst + 1
+    WorkItem* work = nullptr;
+    size_t work_cap = 0;
+    int64_t* work_prefix = nullptr;
+    void* scratch = nullptr;
+    int* flags = nullptr;              // [0] error, [1] counter, [2..3] work count
+    size_t box_bytes = 0;              // p2g node boxes
+    std::vector<size_t> slot_smem;     // g2p dynamic shared memory per slot
+    int max_per_sm = 1;                // resident CTAs per SM (all launches of the plan)
+    int ctas_per_sm = 1;
+    int64_t item = 0;                  // particles per work item
+};
+
+namespace {
+
+constexpr int64_t kMinBatchItem = 256;
+
+void batch_free(cgx_batch* b) {
+    if (!b) return;
+    cudaFree(b->geoms);
+    cudaFree(b->offs);
+    cudaFree(b->tile_base);
+    cudaFree(b->work);
+    cudaFree(b->work_prefix);
+    cudaFree(b->scratch);
+    cudaFree(b->flags);
+    delete b;
+}
+
+cgx_status batch_run(cgx_batch* b, unsigned flags, cudaStream_t st) {
+    const TiledParams& prm = b->prm;
+    const bool halo = b->any_periodic && !(flags & CGX_FLAG_SKIP_HALO);
+    const int n_arrays = prm.n_arrays;
+    if (flags & CGX_FLAG_CHECK_BOUNDS) CGX_CUDA(cudaMemsetAsync(b->flags, 0, sizeof(int), st));
+    if (!b->p2g && halo)
+        for (int i = 0; i < b->n_inst; ++i)
+            if (::any_periodic(b->meshes[i]))
+                for (int a = 0; a < n_arrays; ++a)
+                    CGX_CUDA(launch_halo(to_halo(b->meshes[i], b->arrays[size_t(i) * n_arrays + a]), kHaloGather,
+                                         b->h->sms, st));
+    CGX_CUDA(build_batch_work_items(b->offs, b->tile_base, b->n_inst, b->total_tiles, b->item, b->work_prefix, b->work,
+                                    reinterpret_cast<int64_t*>(b->flags + 2), b->scratch, st, b->h->sms));
+    const int blocks = b->h->sms * b->ctas_per_sm;
+    if (b->p2g) {
+        CGX_CUDA(cudaMemsetAsync(b->flags + 1, 0, sizeof(int), st));
+        CGX_CUDA(launch_p2g_tiled_prepared(prm, b->order, true, blocks, b->box_bytes, st));
+    } else {
+        for (int a = 0; a < n_arrays; ++a) {
+            TiledParams one = prm;
+            one.arrays[a].smem_offset = 0;
+            CGX_CUDA(cudaMemsetAsync(b->flags + 1, 0, sizeof(int), st));
+            CGX_CUDA(launch_g2p_tiled_prepared(one, b->order, a, true, blocks, b->slot_smem[a], st));
+        }
+    }
+    if (b->p2g && halo)
+        for (int i = 0; i < b->n_inst; ++i)
+            if (::any_periodic(b->meshes[i]))
+                for (int a = 0; a < n_arrays; ++a)
+                    CGX_CUDA(launch_halo(to_halo(b->meshes[i], b->arrays[size_t(i) * n_arrays + a]),
+                                         kHaloScatterSum, b->h->sms, st));
+    if (flags & CGX_FLAG_CHECK_BOUNDS) {
+        int host_flag = 0;
+        CGX_CUDA(cudaMemcpyAsync(&host_flag, b->flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CGX_CUDA(cudaStreamSynchronize(st));
+        if (host_flag & (1 << CGX_ERR_OUT_OF_BOUNDS))
+            return fail(CGX_ERR_OUT_OF_BOUNDS, "a point's stencil left the ghosted index space; it was skipped");
+    }
+    return CGX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cgx_status cgx_batch_plan_create(cgx_handle h, const cgx_instance* inst, int n_inst, int spline_order,
+                                 const cgx_op* ops, int n_ops, int p2g, cgx_batch_plan* out) {
+    if (!out) return fail(CGX_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    if (!inst || n_inst < 1) return fail(CGX_ERR_INVALID_ARG, "need at least one instance");
+    if (spline_order < 1 || spline_order > 3) return fail(CGX_ERR_NOT_SUPPORTED, "batched launches take spline order 1-3");
+    if (!ops || n_ops < 1 || n_ops > CGX_BATCH_MAX_OPS) return fail(CGX_ERR_INVALID_ARG, "n_ops must be in [1, 8]");
+    const bool is_p2g = p2g != 0;
+    // Per instance: the cgx_op list with its own buffers; checks as cgx_p2g / cgx_g2p.
+    std::vector<cgx_op> iops(size_t(n_inst) * n_ops);
+    for (int i = 0; i < n_inst; ++i) {
+        const cgx_instance& I = inst[i];
+        cgx_status s = check_mesh(&I.mesh);
+        if (s) return s;
+        if (I.num_point < 0) return fail(CGX_ERR_INVALID_ARG, "num_point must be >= 0");
+        s = check_field(&I.points, "points");
+        if (s) return s;
+        if (I.points.dtype != CGX_F64) return fail(CGX_ERR_INVALID_ARG, "point coordinates must be double (CGX_F64)");
+        if (!I.tiling.tile_offsets || I.tiling.spline_order != spline_order || I.tiling.tile[0] != kTiledTile ||
+            I.tiling.tile[1] != kTiledTile || I.tiling.tile[2] != kTiledTile)
+            return fail(CGX_ERR_INVALID_ARG, "every instance needs a tiling of this spline order with tile 8x8x8");
+        for (int o = 0; o < n_ops; ++o) {
+            cgx_op& op = iops[size_t(i) * n_ops + o];
+            op = ops[o];
+            op.x = I.x[o];
+            op.array = I.array[o];
+        }
+        s = check_ops(&iops[size_t(i) * n_ops], n_ops, is_p2g, true);
+        if (s) return s;
+    }
+    cgx_batch* b = new cgx_batch();
+    b->h = h;
+    b->p2g = is_p2g;
+    b->order = spline_order;
+    b->n_inst = n_inst;
+    if (!setup_tiled(b->prm, iops.data(), n_ops, spline_order, is_p2g)) {
+        delete b;
+        return fail(CGX_ERR_NOT_SUPPORTED, "the operators do not fit the tiled kernels (FP32 point fields, shared memory)");
+    }
+    const int n_arrays = b->prm.n_arrays;
+    std::vector<TiledGeom> geoms(n_inst);
+    std::vector<const int64_t*> offs(n_inst);
+    std::vector<int64_t> base(size_t(n_inst) + 1, 0);
+    b->meshes.resize(n_inst);
+    b->arrays.resize(size_t(n_inst) * n_arrays);
+    for (int i = 0; i < n_inst; ++i) {
+        const cgx_op* io = &iops[size_t(i) * n_ops];
+        TiledParams mine;
+        setup_tiled(mine, io, n_ops, spline_order, is_p2g);
+        for (int o = 0; o < n_ops; ++o) {
+            const int slot = b->prm.ops[o].slot;
+            if (mine.ops[o].slot != slot || io[o].array.dofs != iops[o].array.dofs ||
+                io[o].array.dtype != iops[o].array.dtype || io[o].x.dtype != iops[o].x.dtype) {
+                delete b;
+                return fail(CGX_ERR_INVALID_ARG, "instances differ in array sharing, dofs or dtypes");
+            }
+            b->arrays[size_t(i) * n_arrays + slot] = io[o].array;
+        }
+        fill_geom(geoms[i], b->prm, inst[i].mesh, inst[i].points, io, n_ops, inst[i].tiling, spline_order);
+        b->meshes[i] = inst[i].mesh;
+        b->any_periodic |= ::any_periodic(inst[i].mesh);
+        offs[i] = inst[i].tiling.tile_offsets;
+        const int64_t nt = cgx_tiling_num_offsets(&inst[i].tiling) - 1;
+        base[i + 1] = base[i] + nt;
+        b->total_points += inst[i].num_point;
+    }
+    b->total_tiles = base[n_inst];
+    b->item = kChunk;
+    b->work_cap = size_t(b->total_tiles + b->total_points / kMinBatchItem + 1);
+    cudaError_t e = cudaMalloc(&b->geoms, sizeof(TiledGeom) * n_inst);
+    if (e == cudaSuccess) e = cudaMalloc(&b->offs, sizeof(int64_t*) * n_inst);
+    if (e == cudaSuccess) e = cudaMalloc(&b->tile_base, sizeof(int64_t) * (n_inst + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->work, sizeof(WorkItem) * b->work_cap);
+    if (e == cudaSuccess) e = cudaMalloc(&b->work_prefix, sizeof(int64_t) * size_t(b->total_tiles + 1));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->scratch, scan_scratch_bytes(b->total_tiles) + size_t(b->total_tiles) * 4 + 1024);
+    if (e == cudaSuccess) e = cudaMalloc(&b->flags, 64);
+    if (e == cudaSuccess) e = cudaMemset(b->flags, 0, 64);
+    if (e == cudaSuccess) e = cudaMemcpy(b->geoms, geoms.data(), sizeof(TiledGeom) * n_inst, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->offs, offs.data(), sizeof(int64_t*) * n_inst, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->tile_base, base.data(), sizeof(int64_t) * (n_inst + 1), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        batch_free(b);
+        return cuda_fail(e, "cgx_batch_plan_create");
+    }
+    TiledParams& prm = b->prm;
+    prm.instances = b->geoms;
+    prm.num_point = b->total_points;
+    prm.work = b->work;
+    prm.work_count = reinterpret_cast<const int64_t*>(b->flags + 2);
+    prm.work_counter = b->flags + 1;
+    prm.error_flag = b->flags;
+    // Prepare every kernel of the plan now, so executing it never touches
+    // kernel attributes (and can be captured into a graph).
+    int per_sm = 1 << 30;
+    if (is_p2g) {
+        b->box_bytes = size_t(prm.smem_floats) * sizeof(float);
+        int p = 0;
+        e = prepare_p2g_tiled(prm, spline_order, true, b->box_bytes, &p);
+        per_sm = p;
+    } else {
+        b->slot_smem.resize(n_arrays);
+        for (int a = 0; a < n_arrays && e == cudaSuccess; ++a) {
+            TiledParams one = prm;
+            one.arrays[a].smem_offset = 0;
+            b->slot_smem[a] = g2p_tiled_smem(prm, a);
+            int p = 0;
+            e = prepare_g2p_tiled(one, spline_order, a, true, b->slot_smem[a], &p);
+            per_sm = p < per_sm ? p : per_sm;
+        }
+    }
+    if (e != cudaSuccess || per_sm < 1) {
+        batch_free(b);
+        return e != cudaSuccess ? cuda_fail(e, "cgx_batch_plan_create") : fail(CGX_ERR_NOT_SUPPORTED, "kernel cannot run");
+    }
+    b->max_per_sm = per_sm;
+    b->ctas_per_sm = per_sm;
+    *out = b;
+    return CGX_OK;
+}
+
+cgx_status cgx_batch_plan_destroy(cgx_batch_plan plan) {
+    batch_free(plan);
+    return CGX_OK;
+}
+
+cgx_status cgx_batch_execute(cgx_batch_plan plan, unsigned flags, void* stream) {
+    if (!plan) return fail(CGX_ERR_INVALID_ARG, "plan is NULL");
+    return batch_run(plan, flags, reinterpret_cast<cudaStream_t>(stream));
+}
+
+cgx_status cgx_batch_get_config(cgx_batch_plan plan, int64_t* item_particles, int* ctas_per_sm) {
+    if (!plan) return fail(CGX_ERR_INVALID_ARG, "plan is NULL");
+    if (item_particles) *item_particles = plan->item;
+    if (ctas_per_sm) *ctas_per_sm = plan->ctas_per_sm;
+    return CGX_OK;
+}
+
+cgx_status cgx_batch_set_config(cgx_batch_plan plan, int64_t item_particles, int ctas_per_sm) {
+    if (!plan) return fail(CGX_ERR_INVALID_ARG, "plan is NULL");
+    // p2g work items are staged whole in shared memory: at most kChunk particles
+    const int64_t max_item = plan->p2g ? kChunk : (int64_t(1) << 20);
+    if (item_particles < kMinBatchItem || item_particles > max_item)
+        return fail(CGX_ERR_INVALID_ARG, "item_particles out of range");
+    if (ctas_per_sm < 1 || ctas_per_sm > plan->max_per_sm)
+        return fail(CGX_ERR_INVALID_ARG, "ctas_per_sm must be in [1, resident CTAs per SM]");
+    plan->item = item_particles;
+    plan->ctas_per_sm = ctas_per_sm;
+    return CGX_OK;
+}
+
+cgx_status cgx_batch_autotune(cgx_batch_plan plan, void* stream, double* best_ms) {
+    if (!plan) return fail(CGX_ERR_INVALID_ARG, "plan is NULL");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t items[] = {256, 512, 1024, 2048, 4096};
+    cudaEvent_t e0, e1;
+    CGX_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_fail(ce, "cudaEventCreate");
+    }
+    float best = -1.0f;
+    int64_t best_item = plan->item;
+    int best_ctas = plan->ctas_per_sm;
+    cgx_status s = CGX_OK;
+    for (int64_t item : items) {
+        if (plan->p2g && item > kChunk) continue;
+        for (int c = 1; c <= plan->max_per_sm && s == CGX_OK; ++c) {
+            plan->item = item;
+            plan->ctas_per_sm = c;
+            s = batch_run(plan, 0, st);  // warm-up (work list, caches)
+            if (s) break;
+            float total = 0.0f;
+            for (int rep = 0; rep < 3 && s == CGX_OK; ++rep) {
+                cudaEventRecord(e0, st);
+                s = batch_run(plan, 0, st);
+                cudaEventRecord(e1, st);
+                ce = cudaEventSynchronize(e1);
+                if (ce != cudaSuccess) s = cuda_fail(ce, "cudaEventSynchronize");
+                float ms = 0.0f;
+                if (s == CGX_OK) cudaEventElapsedTime(&ms, e0, e1);
+                total += ms;
+            }
+            if (s == CGX_OK && (best < 0.0f || total < best)) {
+                best = total;
+                best_item = item;
+                best_ctas = c;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    plan->item = best_item;
+    plan->ctas_per_sm = best_ctas;
+    if (best_ms) *best_ms = best < 0.0f ? 0.0 : double(best) / 3.0;
+    return s;
 }
 
 }  // extern "C"

@@ -33,13 +33,13 @@ struct TiledArray {
     int32_t reserved;
 };
 
-// A unit of tiled work: particles [begin, end) of the tile-major order, all
-// filed under tile `tile`.
+// A unit of tiled work: particles [begin, end) of the tile-major order of
+// instance `instance` (0 for a single launch), all filed under tile `tile`.
 struct WorkItem {
     int64_t begin;
     int64_t end;
     int32_t tile;
-    int32_t reserved;
+    int32_t instance;
 };
 
 // One accumulation channel of a tiled p2g launch: a dof of a target array
@@ -78,15 +78,27 @@ constexpr int kTiledTile = 8;
 constexpr int kMaxChannels = 24;
 constexpr int kMaxGroups = 16;
 
-struct TiledParams {
+// The mesh and buffers of one instance of a tiled launch. A single launch
+// carries one in TiledParams::geom; a batched launch (many independent
+// meshes of the same operator structure) reads one per work item from
+// TiledParams::instances.
+struct TiledGeom {
     DMesh mesh;
     double c0[3];  // -low * rdx + (0.5 for even orders): t = fma(x, rdx, c0)
+    int32_t num_tiles[3];
+    int32_t reserved;
     DField points;
+    DField x[kMaxOps];    // point field of operator o
+    DArray arr[kMaxOps];  // distinct grid array `slot`
+};
+
+struct TiledParams {
+    TiledGeom geom;
+    const TiledGeom* instances;  // device; null for a single instance
     int64_t num_point;
     int32_t n_ops;
     int32_t n_arrays;
     int32_t tile[3];
-    int32_t num_tiles[3];
     int32_t box[3];        // node box per tile: tile + num_knot - 1
     int32_t box_nodes;     // box[0] * box[1] * box[2]
     int32_t smem_floats;   // floats of shared memory used for node boxes
@@ -159,6 +171,20 @@ cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int 
 // shared offset 0).
 cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sms, size_t smem_bytes, cudaStream_t st);
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem_bytes, cudaStream_t st);
+// Two-step form of the tiled launches for plans that are launched many
+// times (and may be captured into a CUDA graph): prepare once (sets the
+// kernel's shared-memory limit, reports resident CTAs per SM), then launch
+// with an explicit CTA count. `batched` selects the kernels that read
+// TiledParams::instances. For p2g, `smem_bytes` is the node-box bytes as in
+// p2g_tiled_smem; for g2p it is the full dynamic shared memory.
+cudaError_t prepare_p2g_tiled(const TiledParams& prm, int order, bool batched, size_t box_bytes, int* per_sm);
+cudaError_t launch_p2g_tiled_prepared(const TiledParams& prm, int order, bool batched, int blocks, size_t box_bytes,
+                                      cudaStream_t st);
+cudaError_t prepare_g2p_tiled(const TiledParams& prm, int order, int slot, bool batched, size_t smem, int* per_sm);
+cudaError_t launch_g2p_tiled_prepared(const TiledParams& prm, int order, int slot, bool batched, int blocks,
+                                      size_t smem, cudaStream_t st);
+// Dofs gathered (1 or 3) and whether gradient sums are needed for array `slot`.
+void g2p_slot_need(const TiledParams& prm, int slot, int& ndof, bool& grad);
 // Channels per group of the tiled p2g kernel for a spline order.
 int p2g_group_capacity(int order, bool gradient);
 // Dynamic shared memory of the tiled g2p kernel for array `slot` (huge when
@@ -190,6 +216,13 @@ cudaError_t permute_field(const uint64_t* perm, int64_t begin, int64_t end, cons
                           cudaStream_t st, int sms);
 cudaError_t tile_keys(const DMesh& mesh, const DField& pts, int64_t n, int order, const int32_t* tile,
                       const int32_t* num_tiles, uint32_t* keys, int32_t* tile_counts, cudaStream_t st, int sms);
+// Work items of many instances in one list (instance-major): tile_offsets[i]
+// (device array of device pointers) are instance i's tile offsets and
+// tile_base (device, n_inst + 1 entries) the prefix sum of the instances'
+// tile counts. Scratch: scan_scratch_bytes(total_tiles) + total_tiles * 4.
+cudaError_t build_batch_work_items(const int64_t* const* tile_offsets, const int64_t* tile_base, int n_inst,
+                                   int64_t total_tiles, int64_t chunk, int64_t* work_prefix, WorkItem* work,
+                                   int64_t* work_count, void* scan_scratch, cudaStream_t st, int sms);
 cudaError_t build_work_items(const int64_t* tile_offsets, int64_t num_tiles, int64_t chunk, int64_t* work_prefix,
                              WorkItem* work, int64_t* work_count, void* scan_scratch, cudaStream_t st, int sms);
 cudaError_t counts_to_int64_offsets(const int32_t* counts, int64_t n, int64_t* offsets, void* scratch, cudaStream_t st,

@@ -96,35 +96,35 @@ struct ChanSmem {
 };
 
 template <int ORDER>
-__device__ __forceinline__ bool form_from(const TiledParams& prm, const double* x, int* s, float* u) {
+__device__ __forceinline__ bool form_from(const TiledGeom& geo, const double* x, int* s, float* u) {
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        const double t = fma(x[d], geo.mesh.rdx[d], geo.c0[d]);
         int c;
         ok &= split_logical(t, c, u[d]);
         s[d] = c + first_offset(ORDER);
-        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
     return ok;
 }
 
 template <int ORDER>
-__device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, int* s, float* u) {
+__device__ __forceinline__ bool form_point(const TiledGeom& geo, int64_t p, int* s, float* u) {
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(load_field<double>(prm.points, p, d), prm.mesh.rdx[d], prm.c0[d]);
+        const double t = fma(load_field<double>(geo.points, p, d), geo.mesh.rdx[d], geo.c0[d]);
         int c;
         ok &= split_logical(t, c, u[d]);
         s[d] = c + first_offset(ORDER);
-        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
     return ok;
 }
 
-__device__ __forceinline__ float load_src(const TiledParams& prm, const Source& src, int64_t p) {
-    const DField& f = prm.ops[src.op].x;
+__device__ __forceinline__ float load_src(const TiledGeom& geo, const Source& src, int64_t p) {
+    const DField& f = geo.x[src.op];
     const int64_t o = field_base(f, p) + int64_t(src.comp) * f.comp_stride;
     // raw value: the multiplier is applied where the value is used
     return f.dtype == CGX_F64 ? float(__ldg(reinterpret_cast<const double*>(f.data) + o))
@@ -143,7 +143,7 @@ __device__ __forceinline__ float pick(const float* v, int idx) {
 // into the box, or global atomics when the stencil is outside the box. Each
 // lane walks its stencil starting at a different node.
 template <int ORDER, int TILE, int CH, bool GRAD>
-__device__ __forceinline__ void add_direct(const TiledParams& prm, float* box_smem, const ChanSmem* cs, int first,
+__device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGeom& geo, float* box_smem, const ChanSmem* cs, int first,
                                            int count, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
                                            const float (*coef)[3], bool inbox, const int* l, const int* s, int lane) {
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
@@ -164,7 +164,7 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, float* box_sm
             wv = wi * wj * wk;
         }
         const int bnode = inbox ? ((l[0] + i) * BB + (l[1] + j)) * BB + (l[2] + k) : 0;
-        const int64_t gnode = inbox ? 0 : node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+        const int64_t gnode = inbox ? 0 : node_index(geo.mesh, s[0] + i, s[1] + j, s[2] + k);
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
             if (c >= count) break;
@@ -178,7 +178,7 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, float* box_sm
                 atomicAdd(box_smem + e + m.comp_off, v);
             } else {
                 const Channel& ch = prm.channels[first + c];
-                atomic_add_array(prm.arrays[ch.slot].a, gnode, ch.dof, v);
+                atomic_add_array(geo.arr[ch.slot], gnode, ch.dof, v);
             }
         }
         node = (node + 1 == NODES) ? 0 : node + 1;
@@ -270,7 +270,7 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
 // srcs[s * kChunk + i] is raw source s of item particle i; runs[r] is the
 // first particle of run r (runs[n_runs] = item length).
 template <int ORDER, int TILE, bool GRAD>
-__device__ __forceinline__ void process_runs(const TiledParams& prm, float* box_smem, const float4* prep,
+__device__ __forceinline__ void process_runs(const TiledParams& prm, const TiledGeom& geo, float* box_smem, const float4* prep,
                                              const float* srcs, const int* runs, const int* big, int n_big,
                                              const unsigned char* direct, const unsigned* win_mask, int n_win,
                                              int* next, const ChanSmem* cs, int gi, const int* origin,
@@ -325,7 +325,7 @@ __device__ __forceinline__ void process_runs(const TiledParams& prm, float* box_
             const float u[3] = {pu.x, pu.y, pu.z};
             float w[3][K], g[3][K];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+            for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], geo.mesh.rdx_f[d], w[d], g[d]);
             if (windows == kMaxRunWindows) {
                 flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
                 windows = 0;
@@ -352,7 +352,7 @@ __device__ __forceinline__ void process_runs(const TiledParams& prm, float* box_
         const float u[3] = {pu.x, pu.y, pu.z};
         float w[3][K], g[3][K];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+        for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], geo.mesh.rdx_f[d], w[d], g[d]);
         int l[3], s[3];
         const bool inbox = key >= 0;
         if (inbox) {
@@ -363,13 +363,13 @@ __device__ __forceinline__ void process_runs(const TiledParams& prm, float* box_
             for (int d = 0; d < 3; ++d) s[d] = origin[d] + l[d];
         } else {
             float uu[3];
-            form_point<ORDER>(prm, item_begin + i, s, uu);
+            form_point<ORDER>(geo, item_begin + i, s, uu);
         }
-        add_direct<ORDER, TILE, CH, GRAD>(prm, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
+        add_direct<ORDER, TILE, CH, GRAD>(prm, geo, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
     }
 }
 
-template <int ORDER, int TILE>
+template <int ORDER, int TILE, bool BATCHED>
 __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_constant__ TiledParams prm) {
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
     using SH = P2GShape<ORDER>;
@@ -388,6 +388,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     __shared__ int next_run[2 * kMaxGroups];
     __shared__ int warp_sums[kWarps];
     __shared__ int warp_group[kWarps], group_warps[kMaxGroups];
+    __shared__ TiledGeom sgeo;  // instance of the current work item (batched launches)
+    int cur_inst = -1;
+    const TiledGeom& geo = BATCHED ? sgeo : prm.geom;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int c = threadIdx.x; c < prm.n_channels; c += blockDim.x) {
         const Channel ch = prm.channels[c];
@@ -432,12 +435,20 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         const int64_t widx = item_idx;
         if (widx >= nwork) break;
         const WorkItem it = prm.work[widx];
+        if (BATCHED && it.instance != cur_inst) {
+            // all threads are past the previous item's flush (barrier above)
+            const int* src = reinterpret_cast<const int*>(prm.instances + it.instance);
+            int* dst = reinterpret_cast<int*>(&sgeo);
+            for (int i = threadIdx.x; i < int(sizeof(TiledGeom) / 4); i += blockDim.x) dst[i] = src[i];
+            cur_inst = it.instance;
+            __syncthreads();
+        }
         const int len = int(it.end - it.begin);
         int origin[3];
         {
-            const int t2 = it.tile % prm.num_tiles[2];
-            const int t1 = (it.tile / prm.num_tiles[2]) % prm.num_tiles[1];
-            const int t0 = it.tile / (prm.num_tiles[1] * prm.num_tiles[2]);
+            const int t2 = it.tile % geo.num_tiles[2];
+            const int t1 = (it.tile / geo.num_tiles[2]) % geo.num_tiles[1];
+            const int t0 = it.tile / (geo.num_tiles[1] * geo.num_tiles[2]);
             origin[0] = t0 * prm.tile[0];
             origin[1] = t1 * prm.tile[1];
             origin[2] = t2 * prm.tile[2];
@@ -446,7 +457,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         // copies, one component at a time, all in flight together.
         for (int sidx = 0; sidx < prm.n_sources; ++sidx) {
             const Source src = prm.sources[sidx];
-            const DField f = prm.ops[src.op].x;
+            const DField f = geo.x[src.op];
             float* dst = srcs + sidx * kChunk;
             if (f.log2vl == 0 && f.dtype == CGX_F32) {
                 const float* base = reinterpret_cast<const float*>(f.data) + int64_t(src.comp) * f.comp_stride +
@@ -454,7 +465,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int64_t stride = f.soa_stride;
                 for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, base + i * stride);
             } else {
-                for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(prm, src, it.begin + i);
+                for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(geo, src, it.begin + i);
             }
         }
         // Prep: base node key in the box and in-cell offsets of each thread's
@@ -468,7 +479,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             for (int q = 0; q < PER; ++q) {
                 const int i = threadIdx.x * PER + q;
 #pragma unroll
-                for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(prm.points, it.begin + i, d) : 0.0;
+                for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(geo.points, it.begin + i, d) : 0.0;
             }
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
@@ -477,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 if (i >= len) continue;
                 int s[3];
                 float u[3];
-                if (!form_from<ORDER>(prm, xs[q], s, u)) {
+                if (!form_from<ORDER>(geo, xs[q], s, u)) {
                     raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
                 } else {
                     int l[3];
@@ -547,19 +558,19 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int gi = warp_group[warp];
                 if (gi >= 0) {
                     if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                         origin, it.begin, lane);
                     else
-                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                          origin, it.begin, lane);
                 }
             } else {
                 for (int gi = warp; gi < ng; gi += kWarps) {
                     if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                         origin, it.begin, lane);
                     else
-                        process_runs<ORDER, TILE, false>(prm, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                          origin, it.begin, lane);
                 }
             }
@@ -577,12 +588,12 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int bj = (node / BB) % BB;
                 const int bi = node / (BB * BB);
                 const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
-                if (gi >= prm.mesh.ext[0] || gj >= prm.mesh.ext[1] || gk >= prm.mesh.ext[2]) continue;
-                const int64_t gnode = node_index(prm.mesh, gi, gj, gk);
+                if (gi >= geo.mesh.ext[0] || gj >= geo.mesh.ext[1] || gk >= geo.mesh.ext[2]) continue;
+                const int64_t gnode = node_index(geo.mesh, gi, gj, gk);
                 for (int dof = 0; dof < dofs; ++dof) {
                     const int e = node * dofs + dof;
                     const float v = sum[e] + comp[e];
-                    if (v != 0.0f) atomic_add_array(ta.a, gnode, dof, v);
+                    if (v != 0.0f) atomic_add_array(geo.arr[slot], gnode, dof, v);
                 }
             }
         }
@@ -594,19 +605,41 @@ size_t smem_bytes(const TiledParams& prm, size_t box_bytes) {
     return (box_bytes + 15) / 16 * 16 + size_t(kChunk) * sizeof(float4) + size_t(prm.n_sources) * kChunk * sizeof(float);
 }
 
-template <int ORDER>
-cudaError_t launch_order(const TiledParams& prm, int sms, size_t box_bytes, cudaStream_t st) {
-    constexpr int TILE = kTiledTile;
-    const size_t smem = smem_bytes(prm, box_bytes);
-    const void* fn = reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER, TILE>);
+template <int ORDER, bool BATCHED>
+const void* kernel_fn() {
+    return reinterpret_cast<const void*>(&p2g_tiled_kernel<ORDER, kTiledTile, BATCHED>);
+}
+
+const void* pick_fn(int order, bool batched) {
+    switch (order) {
+        case 1: return batched ? kernel_fn<1, true>() : kernel_fn<1, false>();
+        case 2: return batched ? kernel_fn<2, true>() : kernel_fn<2, false>();
+        case 3: return batched ? kernel_fn<3, true>() : kernel_fn<3, false>();
+    }
+    return nullptr;
+}
+
+// Raise the kernel's dynamic shared-memory limit and report how many CTAs
+// fit on one SM (0: the launch cannot run).
+cudaError_t prepare(const void* fn, size_t smem, int* per_sm) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    p2g_tiled_kernel<ORDER, TILE><<<sms * per_sm, kThreads, smem, st>>>(prm);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fn, kThreads, smem);
+}
+
+template <int ORDER, bool BATCHED>
+cudaError_t launch_kernel(const TiledParams& prm, int blocks, size_t smem, cudaStream_t st) {
+    p2g_tiled_kernel<ORDER, kTiledTile, BATCHED><<<blocks, kThreads, smem, st>>>(prm);
     return cudaGetLastError();
+}
+
+cudaError_t launch_any(const TiledParams& prm, int order, bool batched, int blocks, size_t smem, cudaStream_t st) {
+    switch (order) {
+        case 1: return batched ? launch_kernel<1, true>(prm, blocks, smem, st) : launch_kernel<1, false>(prm, blocks, smem, st);
+        case 2: return batched ? launch_kernel<2, true>(prm, blocks, smem, st) : launch_kernel<2, false>(prm, blocks, smem, st);
+        case 3: return batched ? launch_kernel<3, true>(prm, blocks, smem, st) : launch_kernel<3, false>(prm, blocks, smem, st);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -625,12 +658,25 @@ int64_t p2g_tiled_chunk() { return kChunk; }
 size_t p2g_tiled_smem(const TiledParams& prm, size_t box_bytes) { return smem_bytes(prm, box_bytes); }
 
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem, cudaStream_t st) {
-    switch (order) {
-        case 1: return launch_order<1>(prm, sms, smem, st);
-        case 2: return launch_order<2>(prm, sms, smem, st);
-        case 3: return launch_order<3>(prm, sms, smem, st);
-    }
-    return cudaErrorInvalidValue;
+    const void* fn = pick_fn(order, false);
+    if (!fn) return cudaErrorInvalidValue;
+    const size_t bytes = smem_bytes(prm, smem);
+    int per_sm = 0;
+    cudaError_t e = prepare(fn, bytes, &per_sm);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    return launch_any(prm, order, false, sms * per_sm, bytes, st);
+}
+
+cudaError_t prepare_p2g_tiled(const TiledParams& prm, int order, bool batched, size_t box_bytes, int* per_sm) {
+    const void* fn = pick_fn(order, batched);
+    if (!fn) return cudaErrorInvalidValue;
+    return prepare(fn, smem_bytes(prm, box_bytes), per_sm);
+}
+
+cudaError_t launch_p2g_tiled_prepared(const TiledParams& prm, int order, bool batched, int blocks, size_t box_bytes,
+                                      cudaStream_t st) {
+    return launch_any(prm, order, batched, blocks, smem_bytes(prm, box_bytes), st);
 }
 
 }  // namespace cgx

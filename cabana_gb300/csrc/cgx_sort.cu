@@ -335,7 +335,52 @@ __global__ void tile_work_kernel(const int64_t* tile_offsets, int64_t num_tiles,
             it.begin = s;
             it.end = (s + chunk < e) ? s + chunk : e;
             it.tile = int32_t(t);
-            it.reserved = 0;
+            it.instance = 0;
+            work[w] = it;
+        }
+    }
+}
+
+// Batched work lists: flat tile f of all instances belongs to instance i with
+// tile_base[i] <= f < tile_base[i + 1]; offs[i] are that instance's tile
+// offsets.
+__device__ __forceinline__ int instance_of(const int64_t* tile_base, int n_inst, int64_t f) {
+    int lo = 0, hi = n_inst;  // tile_base[lo] <= f < tile_base[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (tile_base[mid] <= f)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void batch_tile_chunks_kernel(const int64_t* const* offs, const int64_t* tile_base, int n_inst,
+                                         int64_t total, int64_t chunk, int32_t* chunks) {
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t f = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; f < total; f += stride) {
+        const int i = instance_of(tile_base, n_inst, f);
+        const int64_t t = f - tile_base[i];
+        const int64_t cnt = offs[i][t + 1] - offs[i][t];
+        chunks[f] = int32_t((cnt + chunk - 1) / chunk);
+    }
+}
+
+__global__ void batch_tile_work_kernel(const int64_t* const* offs, const int64_t* tile_base, int n_inst,
+                                       int64_t total, int64_t chunk, const uint64_t* work_prefix, WorkItem* work) {
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t f = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; f < total; f += stride) {
+        const int i = instance_of(tile_base, n_inst, f);
+        const int64_t t = f - tile_base[i];
+        const int64_t b = offs[i][t], e = offs[i][t + 1];
+        int64_t w = int64_t(work_prefix[f]);
+        for (int64_t s = b; s < e; s += chunk, ++w) {
+            WorkItem it;
+            it.begin = s;
+            it.end = (s + chunk < e) ? s + chunk : e;
+            it.tile = int32_t(t);
+            it.instance = i;
             work[w] = it;
         }
     }
@@ -516,6 +561,22 @@ cudaError_t build_work_items(const int64_t* tile_offsets, int64_t num_tiles, int
     if (e != cudaSuccess) return e;
     tile_work_kernel<<<blocks_for(num_tiles, 256, sms), 256, 0, st>>>(
         tile_offsets, num_tiles, chunk, reinterpret_cast<const uint64_t*>(work_prefix), work);
+    return cudaGetLastError();
+}
+
+cudaError_t build_batch_work_items(const int64_t* const* tile_offsets, const int64_t* tile_base, int n_inst,
+                                   int64_t total_tiles, int64_t chunk, int64_t* work_prefix, WorkItem* work,
+                                   int64_t* work_count, void* scan_scratch, cudaStream_t st, int sms) {
+    char* p = reinterpret_cast<char*>(scan_scratch);
+    int32_t* chunk_counts = reinterpret_cast<int32_t*>(p);
+    p = align_up(p + size_t(total_tiles) * 4, 256);
+    batch_tile_chunks_kernel<<<blocks_for(total_tiles, 256, sms), 256, 0, st>>>(tile_offsets, tile_base, n_inst,
+                                                                                 total_tiles, chunk, chunk_counts);
+    cudaError_t e = exclusive_scan_counts(chunk_counts, total_tiles, reinterpret_cast<uint64_t*>(work_prefix),
+                                          reinterpret_cast<uint64_t*>(work_count), p, sms, st);
+    if (e != cudaSuccess) return e;
+    batch_tile_work_kernel<<<blocks_for(total_tiles, 256, sms), 256, 0, st>>>(
+        tile_offsets, tile_base, n_inst, total_tiles, chunk, reinterpret_cast<const uint64_t*>(work_prefix), work);
     return cudaGetLastError();
 }
 

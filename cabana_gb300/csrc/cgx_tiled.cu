@@ -47,41 +47,41 @@ __device__ __forceinline__ int dev_g2p_comps(int kind) {
 }
 
 template <int ORDER>
-__device__ __forceinline__ bool form_from(const TiledParams& prm, const double* x, int* s, float* u) {
+__device__ __forceinline__ bool form_from(const TiledGeom& geo, const double* x, int* s, float* u) {
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(x[d], prm.mesh.rdx[d], prm.c0[d]);
+        const double t = fma(x[d], geo.mesh.rdx[d], geo.c0[d]);
         int c;
         ok &= split_logical(t, c, u[d]);
         s[d] = c + first_offset(ORDER);
-        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
     return ok;
 }
 
 template <int ORDER>
-__device__ __forceinline__ bool form_point(const TiledParams& prm, int64_t p, int* s, float* u) {
+__device__ __forceinline__ bool form_point(const TiledGeom& geo, int64_t p, int* s, float* u) {
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(load_field<double>(prm.points, p, d), prm.mesh.rdx[d], prm.c0[d]);
+        const double t = fma(load_field<double>(geo.points, p, d), geo.mesh.rdx[d], geo.c0[d]);
         int c;
         ok &= split_logical(t, c, u[d]);
         s[d] = c + first_offset(ORDER);
-        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= prm.mesh.ext[d]);
+        ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
     return ok;
 }
 
 // Gather sums for one array: V[n] = sum W v_n, D[m][n] = sum d_m W v_n.
 template <int ORDER, int TILE, int NDOF, bool GRAD, bool BOXED>
-__device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledArray& ta, const float* box,
+__device__ __forceinline__ void gather_sums(const TiledGeom& geo, const DArray& arr, const float* box,
                                             const int* l, const int* s, const float (*w)[ORDER + 1],
                                             const float (*g)[ORDER + 1], float* V, float (*D)[3]) {
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
-    const int dofs = ta.a.dofs;
+    const int dofs = arr.dofs;
 #pragma unroll
     for (int n = 0; n < NDOF; ++n) {
         V[n] = 0.0f;
@@ -106,9 +106,9 @@ __device__ __forceinline__ void gather_sums(const TiledParams& prm, const TiledA
 #pragma unroll
                     for (int n = 0; n < NDOF; ++n) v[n] = box[node * dofs + n];
                 } else {
-                    const int64_t node = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+                    const int64_t node = node_index(geo.mesh, s[0] + i, s[1] + j, s[2] + k);
 #pragma unroll
-                    for (int n = 0; n < NDOF; ++n) v[n] = load_array<float>(ta.a, node, n);
+                    for (int n = 0; n < NDOF; ++n) v[n] = load_array<float>(arr, node, n);
                 }
 #pragma unroll
                 for (int n = 0; n < NDOF; ++n) {
@@ -185,7 +185,7 @@ __device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, floa
     }
 }
 
-template <int ORDER, int TILE, int NDOF, bool GRAD>
+template <int ORDER, int TILE, int NDOF, bool GRAD, bool BATCHED>
 __global__ void __launch_bounds__(kThreads, 2)
     g2p_tiled_kernel(const __grid_constant__ TiledParams prm, int slot) {
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
@@ -197,6 +197,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     float4* prep = reinterpret_cast<float4*>(smem + box_floats);
     float* out = reinterpret_cast<float*>(prep + kSub);
     __shared__ int item_idx;
+    __shared__ TiledGeom sgeo;  // instance of the current work item (batched launches)
+    int cur_inst = -1;
+    const TiledGeom& geo = BATCHED ? sgeo : prm.geom;
     const int64_t nwork = *prm.work_count;
     while (true) {
         if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
@@ -204,26 +207,35 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int64_t widx = item_idx;
         if (widx >= nwork) break;
         const WorkItem it = prm.work[widx];
+        if (BATCHED && it.instance != cur_inst) {
+            // every thread finished the previous item (barrier after its last store)
+            const int* src = reinterpret_cast<const int*>(prm.instances + it.instance);
+            int* dst = reinterpret_cast<int*>(&sgeo);
+            for (int i = threadIdx.x; i < int(sizeof(TiledGeom) / 4); i += blockDim.x) dst[i] = src[i];
+            cur_inst = it.instance;
+            __syncthreads();
+        }
+        const DArray& arr = geo.arr[slot];
         int origin[3];
         {
-            const int t2 = it.tile % prm.num_tiles[2];
-            const int t1 = (it.tile / prm.num_tiles[2]) % prm.num_tiles[1];
-            const int t0 = it.tile / (prm.num_tiles[1] * prm.num_tiles[2]);
+            const int t2 = it.tile % geo.num_tiles[2];
+            const int t1 = (it.tile / geo.num_tiles[2]) % geo.num_tiles[1];
+            const int t0 = it.tile / (geo.num_tiles[1] * geo.num_tiles[2]);
             origin[0] = t0 * prm.tile[0];
             origin[1] = t1 * prm.tile[1];
             origin[2] = t2 * prm.tile[2];
         }
         // Stage the node box of the source array (coalesced rows of k * dofs).
         {
-            const int dofs = ta.a.dofs;
+            const int dofs = arr.dofs;
             for (int node = threadIdx.x; node < BB * BB * BB; node += blockDim.x) {
                 const int bk = node % BB;
                 const int bj = (node / BB) % BB;
                 const int bi = node / (BB * BB);
                 const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
-                const bool in = gi < prm.mesh.ext[0] && gj < prm.mesh.ext[1] && gk < prm.mesh.ext[2];
-                const int64_t gnode = in ? node_index(prm.mesh, gi, gj, gk) : 0;
-                for (int dof = 0; dof < dofs; ++dof) box[node * dofs + dof] = in ? load_array<float>(ta.a, gnode, dof) : 0.0f;
+                const bool in = gi < geo.mesh.ext[0] && gj < geo.mesh.ext[1] && gk < geo.mesh.ext[2];
+                const int64_t gnode = in ? node_index(geo.mesh, gi, gj, gk) : 0;
+                for (int dof = 0; dof < dofs; ++dof) box[node * dofs + dof] = in ? load_array<float>(arr, gnode, dof) : 0.0f;
             }
         }
         for (int64_t sb = it.begin; sb < it.end; sb += kSub) {
@@ -237,16 +249,17 @@ __global__ void __launch_bounds__(kThreads, 2)
                 for (int o = 0; o < prm.n_ops; ++o) {
                     const DOp& op = prm.ops[o];
                     if (op.slot != slot) continue;
+                    const DField& fx = geo.x[o];
                     const int nc = dev_g2p_comps(op.kind);
                     for (int c = 0; c < nc; ++c, ++col) {
                         float* dst = out + col * kSub;
-                        if (op.x.log2vl == 0) {
-                            const float* src = reinterpret_cast<const float*>(op.x.data) + int64_t(c) * op.x.comp_stride +
-                                               sb * op.x.soa_stride;
-                            const int64_t stride = op.x.soa_stride;
+                        if (fx.log2vl == 0) {
+                            const float* src = reinterpret_cast<const float*>(fx.data) + int64_t(c) * fx.comp_stride +
+                                               sb * fx.soa_stride;
+                            const int64_t stride = fx.soa_stride;
                             for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, src + i * stride);
                         } else {
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_field<float>(op.x, sb + i, c);
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_field<float>(fx, sb + i, c);
                         }
                     }
                 }
@@ -258,7 +271,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                 for (int q = 0; q < PER; ++q) {
                     const int i = threadIdx.x + q * kThreads;
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(prm.points, sb + i, d) : 0.0;
+                    for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(geo.points, sb + i, d) : 0.0;
                 }
 #pragma unroll
                 for (int q = 0; q < PER; ++q) {
@@ -267,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                     int s[3];
                     float u[3];
                     int key;
-                    if (!form_from<ORDER>(prm, xs[q], s, u)) {
+                    if (!form_from<ORDER>(geo, xs[q], s, u)) {
                         raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
                         key = kKeyInvalid;
                     } else {
@@ -293,18 +306,18 @@ __global__ void __launch_bounds__(kThreads, 2)
                 const float u[3] = {pu.x, pu.y, pu.z};
                 float w[3][K], g[3][K];
 #pragma unroll
-                for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], prm.mesh.rdx_f[d], w[d], g[d]);
+                for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], geo.mesh.rdx_f[d], w[d], g[d]);
                 float V[NDOF], D[3][3];
                 int l[3], s[3];
                 if (key >= 0) {
                     l[2] = key % BB;
                     l[1] = (key / BB) % BB;
                     l[0] = key / (BB * BB);
-                    gather_sums<ORDER, TILE, NDOF, GRAD, true>(prm, ta, box, l, s, w, g, V, D);
+                    gather_sums<ORDER, TILE, NDOF, GRAD, true>(geo, arr, box, l, s, w, g, V, D);
                 } else {
                     float uu[3];
-                    form_point<ORDER>(prm, sb + i, s, uu);
-                    gather_sums<ORDER, TILE, NDOF, GRAD, false>(prm, ta, box, l, s, w, g, V, D);
+                    form_point<ORDER>(geo, sb + i, s, uu);
+                    gather_sums<ORDER, TILE, NDOF, GRAD, false>(geo, arr, box, l, s, w, g, V, D);
                 }
                 apply_ops<NDOF>(prm, slot, out, i, V, D);
             }
@@ -315,17 +328,18 @@ __global__ void __launch_bounds__(kThreads, 2)
                 for (int o = 0; o < prm.n_ops; ++o) {
                     const DOp& op = prm.ops[o];
                     if (op.slot != slot) continue;
+                    const DField& fx = geo.x[o];
                     const int nc = dev_g2p_comps(op.kind);
                     for (int c = 0; c < nc; ++c, ++col) {
                         const float* srcv = out + col * kSub;
-                        if (op.x.log2vl == 0) {
-                            float* dst = reinterpret_cast<float*>(op.x.data) + int64_t(c) * op.x.comp_stride +
-                                         sb * op.x.soa_stride;
-                            const int64_t stride = op.x.soa_stride;
+                        if (fx.log2vl == 0) {
+                            float* dst = reinterpret_cast<float*>(fx.data) + int64_t(c) * fx.comp_stride +
+                                         sb * fx.soa_stride;
+                            const int64_t stride = fx.soa_stride;
                             for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i * stride] = srcv[i];
                         } else {
-                            float* data = reinterpret_cast<float*>(op.x.data);
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) data[field_offset(op.x, sb + i, c)] = srcv[i];
+                            float* data = reinterpret_cast<float*>(fx.data);
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) data[field_offset(fx, sb + i, c)] = srcv[i];
                         }
                     }
                 }
@@ -335,26 +349,45 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-template <int ORDER, int NDOF, bool GRAD>
-cudaError_t launch_g2p(const TiledParams& prm, int slot, int sms, size_t smem, cudaStream_t st) {
-    const void* fn = reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER, kTiledTile, NDOF, GRAD>);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    g2p_tiled_kernel<ORDER, kTiledTile, NDOF, GRAD><<<sms * per_sm, kThreads, smem, st>>>(prm, slot);
+// launch == false: raise the shared-memory limit and report the resident
+// CTAs per SM in *per_sm; launch == true: launch `blocks` CTAs.
+template <int ORDER, int NDOF, bool GRAD, bool BATCHED>
+cudaError_t g2p_op(const TiledParams& prm, int slot, bool launch, int blocks, size_t smem, cudaStream_t st,
+                   int* per_sm) {
+    if (!launch) {
+        const void* fn = reinterpret_cast<const void*>(&g2p_tiled_kernel<ORDER, kTiledTile, NDOF, GRAD, BATCHED>);
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fn, kThreads, smem);
+    }
+    g2p_tiled_kernel<ORDER, kTiledTile, NDOF, GRAD, BATCHED><<<blocks, kThreads, smem, st>>>(prm, slot);
     return cudaGetLastError();
 }
 
-template <int ORDER>
-cudaError_t launch_g2p_slot(const TiledParams& prm, int slot, int ndof, bool grad, int sms, size_t smem,
-                            cudaStream_t st) {
-    if (ndof == 3) return grad ? launch_g2p<ORDER, 3, true>(prm, slot, sms, smem, st)
-                               : launch_g2p<ORDER, 3, false>(prm, slot, sms, smem, st);
-    return grad ? launch_g2p<ORDER, 1, true>(prm, slot, sms, smem, st)
-                : launch_g2p<ORDER, 1, false>(prm, slot, sms, smem, st);
+template <int ORDER, bool BATCHED>
+cudaError_t g2p_shape(const TiledParams& prm, int slot, int ndof, bool grad, bool launch, int blocks, size_t smem,
+                      cudaStream_t st, int* per_sm) {
+    if (ndof == 3)
+        return grad ? g2p_op<ORDER, 3, true, BATCHED>(prm, slot, launch, blocks, smem, st, per_sm)
+                    : g2p_op<ORDER, 3, false, BATCHED>(prm, slot, launch, blocks, smem, st, per_sm);
+    return grad ? g2p_op<ORDER, 1, true, BATCHED>(prm, slot, launch, blocks, smem, st, per_sm)
+                : g2p_op<ORDER, 1, false, BATCHED>(prm, slot, launch, blocks, smem, st, per_sm);
+}
+
+cudaError_t g2p_any(const TiledParams& prm, int order, int slot, bool batched, bool launch, int blocks, size_t smem,
+                    cudaStream_t st, int* per_sm) {
+    int ndof;
+    bool grad;
+    g2p_slot_need(prm, slot, ndof, grad);
+    switch (order) {
+        case 1: return batched ? g2p_shape<1, true>(prm, slot, ndof, grad, launch, blocks, smem, st, per_sm)
+                               : g2p_shape<1, false>(prm, slot, ndof, grad, launch, blocks, smem, st, per_sm);
+        case 2: return batched ? g2p_shape<2, true>(prm, slot, ndof, grad, launch, blocks, smem, st, per_sm)
+                               : g2p_shape<2, false>(prm, slot, ndof, grad, launch, blocks, smem, st, per_sm);
+        case 3: return batched ? g2p_shape<3, true>(prm, slot, ndof, grad, launch, blocks, smem, st, per_sm)
+                               : g2p_shape<3, false>(prm, slot, ndof, grad, launch, blocks, smem, st, per_sm);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -393,15 +426,20 @@ size_t g2p_tiled_smem(const TiledParams& prm, int slot) {
 }
 
 cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sms, size_t smem, cudaStream_t st) {
-    int ndof;
-    bool grad;
-    g2p_slot_need(prm, slot, ndof, grad);
-    switch (order) {
-        case 1: return launch_g2p_slot<1>(prm, slot, ndof, grad, sms, smem, st);
-        case 2: return launch_g2p_slot<2>(prm, slot, ndof, grad, sms, smem, st);
-        case 3: return launch_g2p_slot<3>(prm, slot, ndof, grad, sms, smem, st);
-    }
-    return cudaErrorInvalidValue;
+    int per_sm = 0;
+    cudaError_t e = g2p_any(prm, order, slot, false, false, 0, smem, st, &per_sm);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    return g2p_any(prm, order, slot, false, true, sms * per_sm, smem, st, nullptr);
+}
+
+cudaError_t prepare_g2p_tiled(const TiledParams& prm, int order, int slot, bool batched, size_t smem, int* per_sm) {
+    return g2p_any(prm, order, slot, batched, false, 0, smem, nullptr, per_sm);
+}
+
+cudaError_t launch_g2p_tiled_prepared(const TiledParams& prm, int order, int slot, bool batched, int blocks,
+                                      size_t smem, cudaStream_t st) {
+    return g2p_any(prm, order, slot, batched, true, blocks, smem, st, nullptr);
 }
 
 }  // namespace cgx

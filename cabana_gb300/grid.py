@@ -124,11 +124,17 @@ class Array:
     """Cabana::Grid::Array: a (i, j, k, dof) tensor over the ghosted index
     space (grid/src/Cabana_Grid_Array.hpp:44-300)."""
 
-    def __init__(self, label, layout: ArrayLayout, dtype=torch.float64, device="cuda"):
+    def __init__(self, label, layout: ArrayLayout, dtype=torch.float64, device="cuda", data=None):
         self.label = label
         self._layout = layout
         ext = layout.mesh_params().extents()
-        self._view = torch.zeros(ext + (layout.dofs,), dtype=dtype, device=device)
+        if data is None:
+            self._view = torch.zeros(ext + (layout.dofs,), dtype=dtype, device=device)
+        else:
+            # wrap existing contiguous storage (e.g. a slice of a pooled buffer)
+            if tuple(data.shape) != ext + (layout.dofs,) or not data.is_contiguous():
+                raise ValueError("data must be a contiguous (i, j, k, dof) tensor of the layout's extents")
+            self._view = data
 
     def layout(self):
         return self._layout
@@ -147,8 +153,8 @@ class Array:
         return L.make_mesh(self._layout.mesh_params())
 
 
-def createArray(label, layout, dtype=torch.float64):
-    return Array(label, layout, dtype)
+def createArray(label, layout, dtype=torch.float64, data=None):
+    return Array(label, layout, dtype, data=data)
 
 
 class Halo:
@@ -388,6 +394,78 @@ def g2p_adjoint(array, halo: Optional[Halo], points, num_point, spline: Spline, 
         ab = ab * len(fs)
     _adjoint_call(L.lib().cgx_g2p_adjoint, fs, points, num_point, spline, halo, [None] * len(fs), xb,
                   arrs, ab, points_bar, precision, tiling, handle, stream, check_bounds)
+
+
+@dataclass
+class BatchInstance:
+    """One independent problem of a batch: its points (tile-sorted with
+    `tiling`), point count, and per-functor point field and Array."""
+    points: object
+    num_point: int
+    tiling: "Tiling"
+    fields: list
+    arrays: list
+
+
+class BatchPlan:
+    """Batched p2g (p2g=True) or g2p over many meshes with one work list and
+    one persistent launch (no reference counterpart). `functors` give the
+    operator kinds and multipliers (their fields are ignored); each instance
+    brings its own fields and arrays. execute() neither allocates nor
+    synchronises, so it can be captured into a CUDA graph."""
+
+    def __init__(self, functors, instances, spline: Spline, p2g=True, handle=None):
+        fs = _as_list(functors)
+        if any(f.p2g != p2g for f in fs):
+            raise TypeError("functor direction does not match the plan")
+        self._keep = list(instances)
+        n = len(instances)
+        inst = (L.CgxInstance * n)()
+        for i, b in enumerate(instances):
+            if len(b.fields) != len(fs) or len(b.arrays) != len(fs):
+                raise ValueError("each instance needs one field and one array per functor")
+            inst[i].mesh = b.arrays[0].mesh()
+            inst[i].points = field_descriptor(b.points)
+            inst[i].num_point = int(b.num_point)
+            inst[i].tiling = b.tiling.struct
+            for o in range(len(fs)):
+                inst[i].x[o] = field_descriptor(b.fields[o])
+                inst[i].array[o] = b.arrays[o].descriptor()
+        ops = (L.CgxOp * len(fs))()
+        for o, f in enumerate(fs):
+            ops[o].kind = f.kind
+            ops[o].multiplier = f.multiplier
+        self._handle = handle or L.default_handle()
+        plan = ctypes.c_void_p()
+        L.check(L.lib().cgx_batch_plan_create(self._handle.ptr, inst, n, spline.order, ops, len(fs), int(bool(p2g)),
+                                              ctypes.byref(plan)))
+        self.ptr = plan
+
+    def execute(self, stream=None, halo=True, check_bounds=False):
+        fl = (0 if halo else L.CGX_FLAG_SKIP_HALO) | (L.CGX_FLAG_CHECK_BOUNDS if check_bounds else 0)
+        L.check(L.lib().cgx_batch_execute(self.ptr, fl, _stream(stream)))
+
+    def autotune(self, stream=None):
+        best = ctypes.c_double()
+        L.check(L.lib().cgx_batch_autotune(self.ptr, _stream(stream), ctypes.byref(best)))
+        return best.value
+
+    def config(self):
+        item = ctypes.c_int64()
+        ctas = ctypes.c_int()
+        L.check(L.lib().cgx_batch_get_config(self.ptr, ctypes.byref(item), ctypes.byref(ctas)))
+        return item.value, ctas.value
+
+    def set_config(self, item_particles, ctas_per_sm):
+        L.check(L.lib().cgx_batch_set_config(self.ptr, int(item_particles), int(ctas_per_sm)))
+
+    def __del__(self):
+        try:
+            if getattr(self, "ptr", None):
+                L.lib().cgx_batch_plan_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
 
 
 def last_dispatch(handle=None):

@@ -197,6 +197,68 @@ cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points,
                    int n_ops, int precision, const cgx_tiling* tiling,
                    unsigned flags, void* stream);
 
+/* ---- batched launches (no reference counterpart) ----------------------- */
+
+/*
+ * One independent problem of a batch: its own mesh, its points in the tile
+ * order of its own tiling (cgx_tiling_init + cgx_sort_tiles, tile 8x8x8,
+ * the batch's spline order), and the point field and grid array of each
+ * operator of the batch. Every instance uses the same operator kinds and
+ * multipliers; operators that share an array in one instance must share it
+ * in all, and an operator's array has the same dofs and dtype everywhere.
+ */
+#define CGX_BATCH_MAX_OPS 8
+typedef struct cgx_instance {
+    cgx_mesh mesh;
+    cgx_field points;
+    int64_t num_point;
+    cgx_tiling tiling;
+    cgx_field x[CGX_BATCH_MAX_OPS];
+    cgx_array array[CGX_BATCH_MAX_OPS];
+} cgx_instance;
+
+typedef struct cgx_batch* cgx_batch_plan;
+
+/*
+ * Plan a batched p2g (p2g != 0) or g2p over n_inst instances with the
+ * FP32-compensated tiled kernels (spline order 1-3, FP32 point fields for
+ * g2p). `ops` give the kinds and multipliers; their x / array members are
+ * ignored. The plan uploads the instance table, allocates its work lists
+ * and prepares the kernels; it holds the pointers of `inst`, so the buffers
+ * must outlive it (their contents may change, e.g. a re-sort with
+ * cgx_sort_tiles into the same tile_offsets).
+ */
+cgx_status cgx_batch_plan_create(cgx_handle h, const cgx_instance* inst,
+                                 int n_inst, int spline_order,
+                                 const cgx_op* ops, int n_ops, int p2g,
+                                 cgx_batch_plan* out);
+cgx_status cgx_batch_plan_destroy(cgx_batch_plan plan);
+
+/*
+ * Run the plan on `stream`: one work-list build over all instances and one
+ * persistent launch (g2p: one per distinct array), plus the single-rank
+ * halo step of periodic instances unless CGX_FLAG_SKIP_HALO is set. P2G adds
+ * into the arrays and G2P into the point fields, as cgx_p2g / cgx_g2p do.
+ * Without CGX_FLAG_CHECK_BOUNDS the call neither allocates nor synchronises,
+ * so it can be captured into a CUDA graph.
+ */
+cgx_status cgx_batch_execute(cgx_batch_plan plan, unsigned flags, void* stream);
+
+/*
+ * Autotune the plan on its own data: time each candidate (particles per
+ * work item x resident CTAs per SM) with CUDA events and keep the fastest.
+ * It runs the plan several times, so a p2g plan's arrays (or a g2p plan's
+ * point fields) hold accumulated results afterwards: reset them before use.
+ * best_ms (may be NULL) receives the best time of one execution.
+ */
+cgx_status cgx_batch_autotune(cgx_batch_plan plan, void* stream, double* best_ms);
+
+/* The plan's current settings. */
+cgx_status cgx_batch_get_config(cgx_batch_plan plan, int64_t* item_particles,
+                                int* ctas_per_sm);
+cgx_status cgx_batch_set_config(cgx_batch_plan plan, int64_t item_particles,
+                                int ctas_per_sm);
+
 /* ---- adjoints (no reference counterpart) ------------------------------ */
 
 /*
