@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-instance ensemble leg")
     ap.add_argument("--batch-instances", type=int, default=512)
     ap.add_argument("--batch-seed", type=int, default=5)
+    ap.add_argument("--no-precision", action="store_true", help="skip the large-origin precision sweep")
     return ap.parse_args()
 
 
@@ -317,6 +318,73 @@ def batched_leg(args, dev):
                               "g2p_config": dict(zip(("item_particles", "ctas_per_sm"), gp.config())),
                               "autotune_s": tune_s},
             "speedup": per_ms / batch_ms}
+
+
+def precision_leg(args, dev):
+    """Large-origin precision sweep: 128^3 cells with the low corner at 1e6
+    cell widths, 2^24 uniform particles + 1,677,722 in one sigma-4 clump,
+    Spline<1..3>; P2G ScalarValue(mass) + VectorValue(momentum) +
+    ScalarGradient(mass), G2P ScalarGradient of the mass grid. Errors of the
+    FP32-compensated tiled form against the plain FP64 form."""
+    import torch
+
+    from cabana_gb300 import grid as G
+    from cabana_gb300 import mesh as M
+    cells, off = 128, 1.0e6
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    uni = off + torch.rand((1 << 24, 3), generator=g, device=dev, dtype=torch.float64) * cells
+    centre = off + torch.rand((1, 3), generator=g, device=dev, dtype=torch.float64) * cells
+    clump = centre + torch.randn((1677722, 3), generator=g, device=dev, dtype=torch.float64) * 4.0
+    for _ in range(64):
+        bad = ((clump < off) | (clump >= off + cells)).any(dim=1)
+        nb = int(bad.sum())
+        if nb == 0:
+            break
+        clump[bad] = centre + torch.randn((nb, 3), generator=g, device=dev, dtype=torch.float64) * 4.0
+    pos0 = torch.cat([uni, clump])
+    n = pos0.shape[0]
+    mass0 = torch.rand((n,), generator=g, device=dev) + 0.5
+    mom0 = (mass0[:, None] * torch.randn((n, 3), generator=g, device=dev)).contiguous()
+    lg, mp = M.simple_mesh(cells, 1.0, (off,) * 3, 1)
+    out = {"workload": f"128^3 cells, low corner at 1e6 cell widths, {n} particles (2^24 uniform + 10% in one "
+                       f"sigma-4 clump), P2G mass+momentum+ScalarGradient(mass), G2P ScalarGradient(mass grid)"}
+
+    def run(pos, mass, mom, order, dtype, precision, tiling):
+        arrs = [G.createArray(l, G.createArrayLayout(lg, d, G.Node), dtype) for l, d in (("m", 1), ("p", 3), ("g", 3))]
+        grad = torch.zeros((n, 3), dtype=dtype, device=dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        G.p2g([G.createScalarValueP2G(mass, 1.0), G.createVectorValueP2G(mom, 1.0),
+               G.createScalarGradientP2G(mass, 1.0)], pos, n, G.Spline(order), None, arrs, precision=precision,
+              tiling=tiling)
+        G.g2p(arrs[0], None, pos, n, G.Spline(order), G.createScalarGradientG2P(grad, 1.0), precision=precision,
+              tiling=tiling)
+        b.record()
+        torch.cuda.synchronize()
+        return [x.view() for x in arrs], grad, a.elapsed_time(b)
+
+    def mrel(x, y):
+        return float((x.double() - y.double()).abs().max() / y.double().abs().max())
+
+    for order in (1, 2, 3):
+        til = G.Tiling(mp, order, (8, 8, 8), device=dev)
+        perm = til.sort(pos0, n)
+        pos, mass, mom = pos0[perm].contiguous(), mass0[perm].contiguous(), mom0[perm].contiguous()
+        run(pos, mass, mom, order, torch.float32, G.FP32_COMPENSATED, til)  # warm-up
+        (m32, p32, g32), gr32, t32 = run(pos, mass, mom, order, torch.float32, G.FP32_COMPENSATED, til)
+        (m64, p64, g64), gr64, t64 = run(pos, mass.double(), mom.double(), order, torch.float64, G.PLAIN_FP64, None)
+        msum = mass.double().sum()
+        out[f"spline{order}"] = {
+            "grid_mass_max_rel": mrel(m32, m64), "grid_momentum_max_rel": mrel(p32, p64),
+            "grid_gradient_max_rel": mrel(g32, g64), "point_gradient_max_rel": mrel(gr32, gr64),
+            "mass_conservation_rel": abs(float(m32.double().sum() - msum)) / float(msum),
+            "momentum_conservation_rel": float((p32.double().sum(dim=(0, 1, 2)) - mom.double().sum(dim=0)).abs().max()
+                                               / mom.double().abs().sum(dim=0).max()),
+            "fp32_ms": t32, "fp64_ms": t64}
+        del m32, p32, g32, gr32, m64, p64, g64, gr64
+    return out
 
 
 def time_steps(tr, steps, warmup, barrier):
@@ -589,6 +657,10 @@ def run_ours(args):
     if rank == 0 and not args.no_batch:
         batched = batched_leg(args, dev)
         torch.cuda.empty_cache()
+    precision = None
+    if rank == 0 and not args.no_precision:
+        precision = precision_leg(args, dev)
+        torch.cuda.empty_cache()
 
     cpu = None
     if sample is not None:
@@ -613,7 +685,7 @@ def run_ours(args):
                                   "frac": step_bytes / (ms_per_step / 1000.0) / 1e9 / peak},
                 "kernels_ms": {"p2g": p2g_avg, "g2p": g2p_avg},
                 "cpu_baseline": cpu, "e2e": e2e, "plain_fp64": plain, "errors": errors,
-                "occupancy": occ, "binning_s": bin_s, "batched": batched, "gpu_launches": None, "clocks": clk}
+                "occupancy": occ, "binning_s": bin_s, "batched": batched, "large_origin_precision": precision, "gpu_launches": None, "clocks": clk}
         line["gpu_launches"] = launches_per_step() * args.steps
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -160,6 +160,33 @@ struct SplineKernel {
             w[1] = u;
             g[0] = -r;
             g[1] = r;
+        } else if constexpr (ORDER == 2 && sizeof(T) == 4) {
+            // FP32: the same polynomials in factored form, free of the
+            // cancellation of the expanded ones near the cell ends
+            // (w0 = (1-u)^2 / 2, w2 = u^2 / 2), with the middle weight taken
+            // from the partition of unity so the weights sum to 1 to within
+            // one rounding, with no bias (grid mass is conserved).
+            const T v = T(1) - u;
+            w[0] = T(0.5) * v * v;
+            w[2] = T(0.5) * u * u;
+            w[1] = T(1) - (w[0] + w[2]);
+            g[0] = -v * r;
+            g[2] = u * r;
+            g[1] = -(g[0] + g[2]);
+        } else if constexpr (ORDER == 3 && sizeof(T) == 4) {
+            // FP32 factored cubic B-spline: w0 = (1-u)^3 / 6, w3 = u^3 / 6,
+            // w1 = 2/3 - u^2 (1 - u/2), and w2 from the partition of unity;
+            // the gradient weights likewise sum to zero.
+            const T v = T(1) - u;
+            const T one_sixth = T(1.0 / 6.0);
+            w[0] = one_sixth * v * v * v;
+            w[3] = one_sixth * u * u * u;
+            w[1] = T(2.0 / 3.0) - u * u * (T(1) - T(0.5) * u);
+            w[2] = T(1) - ((w[0] + w[3]) + w[1]);
+            g[0] = T(-0.5) * v * v * r;
+            g[3] = T(0.5) * u * u * r;
+            g[1] = u * (T(1.5) * u - T(2)) * r;
+            g[2] = -((g[0] + g[3]) + g[1]);
         } else if constexpr (ORDER == 2) {
             const T nine_eights = T(9.0 / 8.0);
             T xn = u + T(0.5);
