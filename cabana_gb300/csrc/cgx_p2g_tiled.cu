@@ -18,12 +18,14 @@
 //    spline) and the CTA's 16 warps are shared out among the groups in
 //    proportion to their arithmetic, so a lane holds its group's whole
 //    stencil (27 nodes x channels) in registers.
-//  * Warps pull long runs from a shared counter. A run is walked 32 particles
-//    at a time, one particle per lane, each lane adding its particle into its
-//    registers; at the end of the run the warp reduces the registers across
-//    lanes with a transpose-reduction (each lane ends with 1/32 of the sums)
-//    and adds them into the box with compensated shared atomics -- one shared
-//    atomic per node and channel per run instead of one per particle.
+//  * Long runs are cut into pieces of <= 256 particles, which the group's
+//    warps pull from a shared counter (a dense cell keeps every warp of the
+//    group busy). A piece is walked 32 particles at a time, one particle per
+//    lane, each lane adding its particle into its registers; at the end of
+//    the piece the warp reduces the registers across lanes with a
+//    transpose-reduction (each lane ends with 1/32 of the sums) and adds them
+//    into the box with compensated shared atomics -- one shared atomic per
+//    node and channel per piece instead of one per particle.
 //  * Particles of short runs (and of stencils outside the box) are packed in
 //    aligned 32-particle windows and added directly, each lane walking its
 //    stencil from a different node so lanes of one cell do not collide;
@@ -42,6 +44,10 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 2048;        // particles per work item (host builds items of this size)
 constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
 constexpr int kSmallRun = 12;       // shorter runs add each particle directly
+// Long runs are cut into pieces of at most kPiece particles so that all the
+// warps of a channel group share a dense cell, each piece reduced on its own.
+constexpr int kPiece = 256;
+constexpr int kMaxPieces = kChunk / kSmallRun + kChunk / kPiece + 1;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
 
@@ -262,16 +268,16 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
 }
 
-// One warp of channel group gi first pulls big cell runs (long runs of one
-// base node inside the box) from the group's shared counter and accumulates
-// each in registers, then pulls the aligned 32-particle windows that hold
-// particles of short runs (or of stencils outside the box) and adds those
-// particles directly. prep[i] = (u0, u1, u2, key) of item particle i;
-// srcs[s * kChunk + i] is raw source s of item particle i; runs[r] is the
-// first particle of run r (runs[n_runs] = item length).
+// One warp of channel group gi first pulls pieces of big cell runs (long
+// runs of one base node inside the box; pieces[r] = [begin, end)) from the
+// group's shared counter and accumulates each in registers, then pulls the
+// aligned 32-particle windows that hold particles of short runs (or of
+// stencils outside the box) and adds those particles directly.
+// prep[i] = (u0, u1, u2, key) of item particle i; srcs[s * kChunk + i] is raw
+// source s of item particle i.
 template <int ORDER, int TILE, bool GRAD>
 __device__ __forceinline__ void process_runs(const TiledParams& prm, const TiledGeom& geo, float* box_smem, const float4* prep,
-                                             const float* srcs, const int* runs, const int* big, int n_big,
+                                             const float* srcs, const int2* pieces, int n_pieces,
                                              const unsigned char* direct, const unsigned* win_mask, int n_win,
                                              int* next, const ChanSmem* cs, int gi, const int* origin,
                                              int64_t item_begin, int lane) {
@@ -312,8 +318,8 @@ __device__ __forceinline__ void process_runs(const TiledParams& prm, const Tiled
         int r = 0;
         if (lane == 0) r = atomicAdd(next, 1);
         r = __shfl_sync(0xffffffffu, r, 0);
-        if (r >= n_big) break;
-        const int rb = runs[big[r]], re = runs[big[r] + 1];
+        if (r >= n_pieces) break;
+        const int rb = pieces[r].x, re = pieces[r].y;
         const int key = __float_as_int(prep[rb].w);
         int windows = 0;
         for (int w0 = rb; w0 < re; w0 += 32) {
@@ -381,8 +387,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     __shared__ ChanSmem cs[kMaxChannels];
     __shared__ int item_idx;
     __shared__ int runs[kChunk + 1];
-    __shared__ int big[kChunk];
+    __shared__ int2 pieces[kMaxPieces];
     __shared__ unsigned char direct[kChunk];
+    __shared__ unsigned char run_direct[kChunk];  // per run: its particles are added directly
     __shared__ unsigned win_mask[kChunk / 32 / 32 + 1];
     __shared__ int n_runs, n_big;
     __shared__ int next_run[2 * kMaxGroups];
@@ -473,6 +480,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         // before any is used), then the runs of equal keys.
         constexpr int PER = kChunk / kThreads;
         int keys[PER];
+        int rid[PER];  // run index of each of this thread's particles
         {
             double xs[PER][3];
 #pragma unroll
@@ -530,8 +538,10 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             for (int w2 = 0; w2 < warp; ++w2) wp += warp_sums[w2];
             int pos = wp + x - nstart;
 #pragma unroll
-            for (int q = 0; q < PER; ++q)
+            for (int q = 0; q < PER; ++q) {
                 if (flags & (1 << q)) runs[pos++] = threadIdx.x * PER + q;
+                rid[q] = pos - 1;  // run of particle threadIdx.x * PER + q
+            }
             if (threadIdx.x == kThreads - 1) {
                 n_runs = pos;
                 runs[pos] = len;
@@ -544,13 +554,32 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             const int rb = runs[r], re = runs[r + 1];
             const int key = __float_as_int(prep[rb].w);
             const bool is_big = key >= 0 && re - rb >= kSmallRun;
-            if (is_big) big[atomicAdd(&n_big, 1)] = r;
-            const unsigned char dflag = (!is_big && key != kKeyInvalid) ? 1 : 0;
-            for (int i = rb; i < re; ++i) direct[i] = dflag;
-            if (dflag)
-                for (int wi = rb >> 5; wi <= (re - 1) >> 5; ++wi) atomicOr(&win_mask[wi >> 5], 1u << (wi & 31));
+            if (is_big) {
+                // n_big counts pieces: at most kChunk / kPiece + (number of big runs) <= kMaxPieces
+                const int np = (re - rb + kPiece - 1) / kPiece;
+                const int base = atomicAdd(&n_big, np);
+                for (int q = 0; q < np; ++q)
+                    pieces[base + q] = make_int2(rb + q * kPiece, min(re, rb + (q + 1) * kPiece));
+            }
+            run_direct[r] = (!is_big && key != kKeyInvalid) ? 1 : 0;
         }
-        for (int i = len + threadIdx.x; i < ((len + 31) & ~31); i += blockDim.x) direct[i] = 0;
+        __syncthreads();
+        // Per-particle direct flags and the windows that hold any, each
+        // thread for its own particles (a run's length never serialises).
+        {
+            bool any = false;
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int i = threadIdx.x * PER + q;
+                const unsigned char d = i < len ? run_direct[rid[q]] : 0;
+                direct[i] = d;
+                any |= d != 0;
+            }
+            if (any) {
+                const int wi = (threadIdx.x * PER) >> 5;
+                atomicOr(&win_mask[wi >> 5], 1u << (wi & 31));
+            }
+        }
         __syncthreads();
         {
             const int nbig = n_big, nwin = (len + 31) >> 5;
@@ -558,19 +587,19 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int gi = warp_group[warp];
                 if (gi >= 0) {
                     if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                         origin, it.begin, lane);
                     else
-                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                          origin, it.begin, lane);
                 }
             } else {
                 for (int gi = warp; gi < ng; gi += kWarps) {
                     if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                         origin, it.begin, lane);
                     else
-                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, runs, big, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
+                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
                                                          origin, it.begin, lane);
                 }
             }
