@@ -371,7 +371,7 @@ bool setup_tiled(TiledParams& prm, const cgx_op* ops, int n_ops, int spline_orde
     if (p2g && !plan_channels(prm, ops, n_ops, spline_order)) ok = false;  // too many channel groups
     // node boxes plus per-item staging must fit in one SM's shared memory
     if (p2g) {
-        if (p2g_tiled_smem(prm, size_t(offset) * sizeof(float)) > 210 * 1024) ok = false;  // + ~9 KB static tables
+        if (p2g_tiled_smem(prm, size_t(offset) * sizeof(float)) > p2g_tiled_smem_limit(spline_order)) ok = false;
     } else {
         // g2p_tiled_smem also refuses double point fields
         for (int o = 0; o < n_ops; ++o) prm.ops[o].x.dtype = ops[o].x.dtype;

@@ -192,6 +192,9 @@ int p2g_group_capacity(int order, bool gradient);
 size_t g2p_tiled_smem(const TiledParams& prm, int slot);
 // Particles per work item of the tiled kernels.
 int64_t p2g_tiled_chunk();
+// Largest dynamic shared memory the tiled p2g kernel of a spline order can
+// be launched with on the current device (0 if it cannot be queried).
+size_t p2g_tiled_smem_limit(int order);
 // Dynamic shared memory of the tiled p2g kernel: node boxes + per-item
 // staging of base keys, offsets and sources.
 size_t p2g_tiled_smem(const TiledParams& prm, size_t box_bytes);

@@ -15,12 +15,11 @@
 //  * Operators are lowered to channels: one grid dof that receives, per
 //    point, a * W (value channel) or b . grad W (gradient channel). Channels
 //    are grouped (2 value or 1 gradient channel per group for the quadratic
-//    spline) and the CTA's 16 warps are shared out among the groups in
-//    proportion to their arithmetic, so a lane holds its group's whole
-//    stencil (27 nodes x channels) in registers.
-//  * Long runs are cut into pieces of <= 256 particles, which the group's
-//    warps pull from a shared counter (a dense cell keeps every warp of the
-//    group busy). A piece is walked 32 particles at a time, one particle per
+//    spline) so a lane holds its group's whole stencil (27 nodes x channels)
+//    in registers. The CTA's 16 warps pull units of work -- (piece, group)
+//    and then (window, group) -- from shared counters.
+//  * Runs of two or more particles are cut into pieces of <= 256 particles
+//    (a dense cell keeps every warp busy). A piece is walked 32 particles at a time, one particle per
 //    lane, each lane adding its particle into its registers; at the end of
 //    the piece the warp reduces the registers across lanes with a
 //    transpose-reduction (each lane ends with 1/32 of the sums) and adds them
@@ -43,7 +42,7 @@ constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 2048;        // particles per work item (host builds items of this size)
 constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
-constexpr int kSmallRun = 12;       // shorter runs add each particle directly
+constexpr int kSmallRun = 2;        // shorter runs (single particles) add each particle directly
 // Long runs are cut into pieces of at most kPiece particles so that all the
 // warps of a channel group share a dense cell, each piece reduced on its own.
 constexpr int kPiece = 256;
@@ -135,6 +134,22 @@ __device__ __forceinline__ float load_src(const TiledGeom& geo, const Source& sr
     // raw value: the multiplier is applied where the value is used
     return f.dtype == CGX_F64 ? float(__ldg(reinterpret_cast<const double*>(f.data) + o))
                               : __ldg(reinterpret_cast<const float*>(f.data) + o);
+}
+
+// L2 prefetch of particles [b, e) of a field stored densely per particle
+// (vector length 1, components adjacent); other layouts are left alone.
+__device__ __forceinline__ void prefetch_field_range(const DField& f, int64_t b, int64_t e) {
+    if (f.log2vl != 0 || f.comp_stride != 1) return;
+    const int64_t elt = f.dtype == CGX_F64 ? 8 : 4;
+    const char* base = f.data + b * f.soa_stride * elt;
+    const int64_t bytes = (e - b) * f.soa_stride * elt;
+    for (int64_t o = int64_t(threadIdx.x) * 128; o < bytes; o += int64_t(blockDim.x) * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + o));
+}
+
+__device__ __forceinline__ void prefetch_item(const TiledGeom* g, int n_ops, int64_t b, int64_t e) {
+    prefetch_field_range(g->points, b, e);
+    for (int o = 0; o < n_ops; ++o) prefetch_field_range(g->x[o], b, e);
 }
 
 template <int K>
@@ -268,37 +283,27 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
 }
 
-// One warp of channel group gi first pulls pieces of big cell runs (long
-// runs of one base node inside the box; pieces[r] = [begin, end)) from the
-// group's shared counter and accumulates each in registers, then pulls the
-// aligned 32-particle windows that hold particles of short runs (or of
-// stencils outside the box) and adds those particles directly.
-// prep[i] = (u0, u1, u2, key) of item particle i; srcs[s * kChunk + i] is raw
-// source s of item particle i.
-template <int ORDER, int TILE, bool GRAD>
-__device__ __forceinline__ void process_runs(const TiledParams& prm, const TiledGeom& geo, float* box_smem, const float4* prep,
-                                             const float* srcs, const int2* pieces, int n_pieces,
-                                             const unsigned char* direct, const unsigned* win_mask, int n_win,
-                                             int* next, const ChanSmem* cs, int gi, const int* origin,
-                                             int64_t item_begin, int lane) {
-    using SH = P2GShape<ORDER>;
-    constexpr int BB = TILE + ORDER;
-    constexpr int K = SH::K;
-    constexpr int CH = GRAD ? SH::CG : SH::CV;
-    constexpr int NPAD = GRAD ? SH::NG : SH::NV;
-    constexpr int NS = GRAD ? 3 : 1;  // sources per channel
-    const ChannelGroup grp = prm.groups[gi];
-    const int first = grp.first, count = grp.count;
+// The source rows and multipliers of channel group gi, and the per-lane
+// coefficient load: coef[c][n] = source n of channel c of particle i times
+// its multiplier. srcs[s * kChunk + i] is raw source s of item particle i.
+template <int CH, int NS>
+struct GroupCoef {
+    int first, count;
     int srow[CH][NS];
     float smul[CH][NS];
+    __device__ __forceinline__ GroupCoef(const TiledParams& prm, int gi) {
+        const ChannelGroup grp = prm.groups[gi];
+        first = grp.first;
+        count = grp.count;
 #pragma unroll
-    for (int c = 0; c < CH; ++c)
+        for (int c = 0; c < CH; ++c)
 #pragma unroll
-        for (int n = 0; n < NS; ++n) {
-            srow[c][n] = c < count ? prm.channels[first + c].src[n] : -1;
-            smul[c][n] = srow[c][n] >= 0 ? prm.sources[srow[c][n]].mult : 0.0f;
-        }
-    auto load_coef = [&](int i, bool active, float (*coef)[3]) {
+            for (int n = 0; n < NS; ++n) {
+                srow[c][n] = c < count ? prm.channels[first + c].src[n] : -1;
+                smul[c][n] = srow[c][n] >= 0 ? prm.sources[srow[c][n]].mult : 0.0f;
+            }
+    }
+    __device__ __forceinline__ void load(const float* srcs, int i, bool active, float (*coef)[3]) const {
 #pragma unroll
         for (int c = 0; c < CH; ++c)
 #pragma unroll
@@ -306,27 +311,35 @@ __device__ __forceinline__ void process_runs(const TiledParams& prm, const Tiled
                 const int rr = n < NS ? srow[c][n < NS ? n : 0] : -1;
                 coef[c][n] = (rr >= 0 && active) ? srcs[rr * kChunk + i] * smul[c][n < NS ? n : 0] : 0.0f;
             }
-    };
+    }
+};
 
+// One piece [rb, re) of a big cell run (one base node inside the box) for
+// channel group gi: register accumulation, then one reduction and one
+// compensated shared atomic per node and channel. prep[i] = (u0, u1, u2,
+// key) of item particle i.
+template <int ORDER, int TILE, bool GRAD>
+__device__ __forceinline__ void run_piece(const TiledParams& prm, const TiledGeom& geo, float* box_smem,
+                                          const float4* prep, const float* srcs, int2 piece, const ChanSmem* cs,
+                                          int gi, int lane) {
+    using SH = P2GShape<ORDER>;
+    constexpr int K = SH::K;
+    constexpr int CH = GRAD ? SH::CG : SH::CV;
+    constexpr int NPAD = GRAD ? SH::NG : SH::NV;
+    const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi);
+    const int first = gc.first, count = gc.count;
     float acc[NPAD];
 #pragma unroll
     for (int v = 0; v < NPAD; ++v) acc[v] = 0.0f;
-
-    // Big runs: register accumulation, one flush per run (or per
-    // kMaxRunWindows windows).
-    while (true) {
-        int r = 0;
-        if (lane == 0) r = atomicAdd(next, 1);
-        r = __shfl_sync(0xffffffffu, r, 0);
-        if (r >= n_pieces) break;
-        const int rb = pieces[r].x, re = pieces[r].y;
+    {
+        const int rb = piece.x, re = piece.y;
         const int key = __float_as_int(prep[rb].w);
         int windows = 0;
         for (int w0 = rb; w0 < re; w0 += 32) {
             const int i = w0 + lane;
             const bool active = i < re;
             float coef[CH][3];
-            load_coef(i, active, coef);
+            gc.load(srcs, i, active, coef);
             const float4 pu = active ? prep[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const float u[3] = {pu.x, pu.y, pu.z};
             float w[3][K], g[3][K];
@@ -341,18 +354,28 @@ __device__ __forceinline__ void process_runs(const TiledParams& prm, const Tiled
         }
         flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
     }
-    // Windows with particles of short runs: each lane adds its own particle.
-    while (true) {
-        int wi = 0;
-        if (lane == 0) wi = atomicAdd(next + 1, 1);
-        wi = __shfl_sync(0xffffffffu, wi, 0);
-        if (wi >= n_win) break;
-        if (!(win_mask[wi >> 5] & (1u << (wi & 31)))) continue;
+}
+
+// One aligned 32-particle window wi for channel group gi: each lane whose
+// particle is flagged direct (short run, or stencil outside the box) adds
+// it on its own.
+template <int ORDER, int TILE, bool GRAD>
+__device__ __forceinline__ void run_window(const TiledParams& prm, const TiledGeom& geo, float* box_smem,
+                                           const float4* prep, const float* srcs, const unsigned char* direct,
+                                           int wi, const ChanSmem* cs, int gi, const int* origin,
+                                           int64_t item_begin, int lane) {
+    using SH = P2GShape<ORDER>;
+    constexpr int BB = TILE + ORDER;
+    constexpr int K = SH::K;
+    constexpr int CH = GRAD ? SH::CG : SH::CV;
+    const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi);
+    const int first = gc.first, count = gc.count;
+    {
         const int i = wi * 32 + lane;
         const bool active = direct[i] != 0;
         float coef[CH][3];
-        load_coef(i, active, coef);
-        if (!active) continue;
+        gc.load(srcs, i, active, coef);
+        if (!active) return;
         const float4 pu = prep[i];
         const int key = __float_as_int(pu.w);
         const float u[3] = {pu.x, pu.y, pu.z};
@@ -394,7 +417,6 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     __shared__ int n_runs, n_big;
     __shared__ int next_run[2 * kMaxGroups];
     __shared__ int warp_sums[kWarps];
-    __shared__ int warp_group[kWarps], group_warps[kMaxGroups];
     __shared__ TiledGeom sgeo;  // instance of the current work item (batched launches)
     int cur_inst = -1;
     const TiledGeom& geo = BATCHED ? sgeo : prm.geom;
@@ -407,28 +429,14 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         cs[c].dofs = ta.a.dofs;
     }
     const int ng = prm.n_groups;
-    if (threadIdx.x == 0) {
-        // Share the warps among the groups in proportion to their arithmetic
-        // (a gradient channel costs about twice a value channel).
-        int cost[kMaxGroups];
-        for (int gi = 0; gi < ng; ++gi) {
-            cost[gi] = prm.groups[gi].count * (prm.groups[gi].gradient ? 2 * SH::CV / SH::CG : 1);
-            group_warps[gi] = 1;
-        }
-        for (int left = kWarps - ng; left > 0 && ng > 0; --left) {
-            int best = 0;
-            for (int gi = 1; gi < ng; ++gi)
-                if (cost[gi] * group_warps[best] > cost[best] * group_warps[gi]) best = gi;
-            group_warps[best] += 1;
-        }
-        int w = 0;
-        for (int gi = 0; gi < ng && w < kWarps; ++gi)
-            for (int r = 0; r < group_warps[gi] && w < kWarps; ++r, ++w) warp_group[w] = gi;
-        for (; w < kWarps; ++w) warp_group[w] = -1;
-    }
     const int64_t nwork = *prm.work_count;
+    __shared__ int next_idx;  // the item after the current one (its inputs are prefetched into L2)
+    if (threadIdx.x == 0) next_idx = atomicAdd(prm.work_counter, 1);
     while (true) {
-        if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
+        if (threadIdx.x == 0) {
+            item_idx = next_idx;
+            next_idx = atomicAdd(prm.work_counter, 1);
+        }
         if (threadIdx.x < 2 * kMaxGroups) next_run[threadIdx.x] = 0;
         if (threadIdx.x < kChunk / 32 / 32 + 1) win_mask[threadIdx.x] = 0u;
         if (threadIdx.x == 0) n_big = 0;
@@ -449,6 +457,15 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             for (int i = threadIdx.x; i < int(sizeof(TiledGeom) / 4); i += blockDim.x) dst[i] = src[i];
             cur_inst = it.instance;
             __syncthreads();
+        }
+        {
+            // Pull the next item's coordinates and operator inputs into L2
+            // while this item is processed: its prep then waits on L2, not HBM.
+            const int64_t nidx = next_idx;
+            if (nidx < nwork) {
+                const WorkItem nx = prm.work[nidx];
+                prefetch_item(BATCHED ? prm.instances + nx.instance : &prm.geom, prm.n_ops, nx.begin, nx.end);
+            }
         }
         const int len = int(it.end - it.begin);
         int origin[3];
@@ -582,26 +599,36 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         }
         __syncthreads();
         {
-            const int nbig = n_big, nwin = (len + 31) >> 5;
-            if (ng <= kWarps) {
-                const int gi = warp_group[warp];
-                if (gi >= 0) {
-                    if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
-                                                        origin, it.begin, lane);
-                    else
-                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
-                                                         origin, it.begin, lane);
-                }
-            } else {
-                for (int gi = warp; gi < ng; gi += kWarps) {
-                    if (prm.groups[gi].gradient)
-                        process_runs<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
-                                                        origin, it.begin, lane);
-                    else
-                        process_runs<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, pieces, nbig, direct, win_mask, nwin, next_run + 2 * gi, cs, gi,
-                                                         origin, it.begin, lane);
-                }
+            // Units of work are (piece, group) and then (window, group),
+            // pulled by any warp from two shared counters: every warp stays
+            // busy whatever the mix of value and gradient groups.
+            const int nunit = n_big * ng, nwin = (len + 31) >> 5;
+            while (true) {
+                int u = 0;
+                if (lane == 0) u = atomicAdd(&next_run[0], 1);
+                u = __shfl_sync(0xffffffffu, u, 0);
+                if (u >= nunit) break;
+                const int gi = u % ng;
+                const int2 piece = pieces[u / ng];
+                if (prm.groups[gi].gradient)
+                    run_piece<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
+                else
+                    run_piece<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
+            }
+            const int wunit = nwin * ng;
+            while (true) {
+                int u = 0;
+                if (lane == 0) u = atomicAdd(&next_run[1], 1);
+                u = __shfl_sync(0xffffffffu, u, 0);
+                if (u >= wunit) break;
+                const int gi = u % ng, wi = u / ng;
+                if (!(win_mask[wi >> 5] & (1u << (wi & 31)))) continue;
+                if (prm.groups[gi].gradient)
+                    run_window<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, direct, wi, cs, gi, origin, it.begin,
+                                                  lane);
+                else
+                    run_window<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, direct, wi, cs, gi, origin,
+                                                   it.begin, lane);
             }
         }
         __syncthreads();
@@ -685,6 +712,23 @@ int p2g_group_capacity(int order, bool gradient) {
 int64_t p2g_tiled_chunk() { return kChunk; }
 
 size_t p2g_tiled_smem(const TiledParams& prm, size_t box_bytes) { return smem_bytes(prm, box_bytes); }
+
+size_t p2g_tiled_smem_limit(int order) {
+    // the device's opt-in shared memory per block minus the kernel's static
+    // tables (the larger of the single and batched instantiations)
+    const void* fns[2] = {pick_fn(order, false), pick_fn(order, true)};
+    int dev = 0, optin = 0;
+    if (!fns[0] || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return 0;
+    size_t stat = 0;
+    for (const void* fn : fns) {
+        cudaFuncAttributes a;
+        if (cudaFuncGetAttributes(&a, fn) != cudaSuccess) return 0;
+        stat = a.sharedSizeBytes > stat ? a.sharedSizeBytes : stat;
+    }
+    return size_t(optin) > stat ? size_t(optin) - stat : 0;
+}
 
 cudaError_t launch_p2g_tiled(const TiledParams& prm, int order, int sms, size_t smem, cudaStream_t st) {
     const void* fn = pick_fn(order, false);
