@@ -81,7 +81,7 @@ __device__ __forceinline__ void gather_sums(const TiledGeom& geo, const DArray& 
                                             const float (*g)[ORDER + 1], float* V, float (*D)[3]) {
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
-    const int dofs = arr.dofs;
+    static_assert(NDOF == 1 || NDOF == 3, "one or three gathered dofs");
 #pragma unroll
     for (int n = 0; n < NDOF; ++n) {
         V[n] = 0.0f;
@@ -102,9 +102,16 @@ __device__ __forceinline__ void gather_sums(const TiledGeom& geo, const DArray& 
             for (int k = 0; k < K; ++k) {
                 float v[NDOF];
                 if (BOXED) {
+                    // box nodes are padded to 4 floats for 3 dofs: one 16-byte load per node
                     const int node = ((l[0] + i) * BB + (l[1] + j)) * BB + (l[2] + k);
-#pragma unroll
-                    for (int n = 0; n < NDOF; ++n) v[n] = box[node * dofs + n];
+                    if constexpr (NDOF == 3) {
+                        const float4 q = reinterpret_cast<const float4*>(box)[node];
+                        v[0] = q.x;
+                        v[1 < NDOF ? 1 : 0] = q.y;
+                        v[2 < NDOF ? 2 : 0] = q.z;
+                    } else {
+                        v[0] = box[node];
+                    }
                 } else {
                     const int64_t node = node_index(geo.mesh, s[0] + i, s[1] + j, s[2] + k);
 #pragma unroll
@@ -191,8 +198,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
     extern __shared__ __align__(16) float smem[];
-    const TiledArray& ta = prm.arrays[slot];
-    const int box_floats = ((BB * BB * BB) * ta.a.dofs + 3) & ~3;
+    constexpr int BSTR = NDOF == 3 ? 4 : 1;  // floats per box node
+    constexpr int box_floats = ((BB * BB * BB) * BSTR + 3) & ~3;
     float* box = smem;
     float4* prep = reinterpret_cast<float4*>(smem + box_floats);
     float* out = reinterpret_cast<float*>(prep + kSub);
@@ -225,17 +232,29 @@ __global__ void __launch_bounds__(kThreads, 2)
             origin[1] = t1 * prm.tile[1];
             origin[2] = t2 * prm.tile[2];
         }
-        // Stage the node box of the source array (coalesced rows of k * dofs).
+        // Stage the gathered dofs of the node box (rows of k are contiguous
+        // in the array), as asynchronous copies that complete with the first
+        // sub-batch's copies; nodes beyond the mesh read as zero.
         {
-            const int dofs = arr.dofs;
+            const float* adata = reinterpret_cast<const float*>(arr.data);
             for (int node = threadIdx.x; node < BB * BB * BB; node += blockDim.x) {
                 const int bk = node % BB;
                 const int bj = (node / BB) % BB;
                 const int bi = node / (BB * BB);
                 const int gi = origin[0] + bi, gj = origin[1] + bj, gk = origin[2] + bk;
                 const bool in = gi < geo.mesh.ext[0] && gj < geo.mesh.ext[1] && gk < geo.mesh.ext[2];
-                const int64_t gnode = in ? node_index(geo.mesh, gi, gj, gk) : 0;
-                for (int dof = 0; dof < dofs; ++dof) box[node * dofs + dof] = in ? load_array<float>(arr, gnode, dof) : 0.0f;
+                if (in && arr.dtype == CGX_F32) {
+                    const int64_t gnode = node_index(geo.mesh, gi, gj, gk);
+#pragma unroll
+                    for (int dof = 0; dof < NDOF; ++dof) cp_async4(box + node * BSTR + dof, adata + gnode * arr.dofs + dof);
+                } else if (in) {  // double arrays are rounded to FP32 on the way
+                    const int64_t gnode = node_index(geo.mesh, gi, gj, gk);
+#pragma unroll
+                    for (int dof = 0; dof < NDOF; ++dof) box[node * BSTR + dof] = load_array<float>(arr, gnode, dof);
+                } else {
+#pragma unroll
+                    for (int dof = 0; dof < NDOF; ++dof) box[node * BSTR + dof] = 0.0f;
+                }
             }
         }
         for (int64_t sb = it.begin; sb < it.end; sb += kSub) {
@@ -421,7 +440,10 @@ size_t g2p_tiled_smem(const TiledParams& prm, int slot) {
     // Point fields are staged as FP32: double fields, or too many components,
     // are left to the point-parallel kernel.
     if (cols > kMaxOutCols || f64_out) return size_t(1) << 30;
-    const size_t box = size_t((prm.box_nodes * prm.arrays[slot].a.dofs + 3) & ~3) * sizeof(float);
+    int ndof;
+    bool grad;
+    g2p_slot_need(prm, slot, ndof, grad);
+    const size_t box = size_t((prm.box_nodes * (ndof == 3 ? 4 : 1) + 3) & ~3) * sizeof(float);
     return box + size_t(kSub) * sizeof(float4) + size_t(cols) * kSub * sizeof(float);
 }
 
