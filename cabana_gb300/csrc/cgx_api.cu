@@ -307,11 +307,21 @@ bool plan_channels(TiledParams& prm, const cgx_op* ops, int n_ops, int order) {
     return true;
 }
 
-const int64_t kChunk = p2g_tiled_chunk();  // work-item size shared by the tiled kernels
+const int64_t kChunk = p2g_tiled_chunk();  // largest work item of the tiled kernels
+
+// Particles per work item for one call: large items flush the node box less
+// often, small ones balance small problems; aim for >= 4 items per SM.
+int64_t item_particles(const cgx_context* h, int64_t num_point) {
+    const int64_t want = num_point / (int64_t(h->sms) * 4);
+    int64_t item = 2048;
+    while (item < want && item < kChunk) item *= 2;
+    return item;
+}
 
 cgx_status build_work(cgx_context* h, const cgx_tiling& t, int64_t num_point, cudaStream_t st) {
     const int64_t nt = int64_t(t.num_tiles[0]) * t.num_tiles[1] * t.num_tiles[2];
-    const size_t cap = size_t(nt + num_point / kChunk + 1);
+    const int64_t item = item_particles(h, num_point);
+    const size_t cap = size_t(nt + num_point / item + 1);
     if (cap > h->work_cap) {
         if (h->work) cudaFree(h->work);
         h->work = nullptr;
@@ -328,7 +338,7 @@ cgx_status build_work(cgx_context* h, const cgx_tiling& t, int64_t num_point, cu
     }
     cgx_status s = ensure_ws(h, size_t(nt) * 4 + 512 + scan_scratch_bytes(nt));
     if (s) return s;
-    CGX_CUDA(build_work_items(t.tile_offsets, nt, kChunk, h->work_prefix, h->work,
+    CGX_CUDA(build_work_items(t.tile_offsets, nt, item, h->work_prefix, h->work,
                               reinterpret_cast<int64_t*>(h->flags + 2), h->ws, st, h->sms));
     return CGX_OK;
 }
@@ -1182,8 +1192,7 @@ cgx_status cgx_batch_get_config(cgx_batch_plan plan, int64_t* item_particles, in
 
 cgx_status cgx_batch_set_config(cgx_batch_plan plan, int64_t item_particles, int ctas_per_sm) {
     if (!plan) return fail(CGX_ERR_INVALID_ARG, "plan is NULL");
-    // p2g work items are staged whole in shared memory: at most kChunk particles
-    const int64_t max_item = plan->p2g ? kChunk : (int64_t(1) << 20);
+    const int64_t max_item = int64_t(1) << 20;
     if (item_particles < kMinBatchItem || item_particles > max_item)
         return fail(CGX_ERR_INVALID_ARG, "item_particles out of range");
     if (ctas_per_sm < 1 || ctas_per_sm > plan->max_per_sm)
@@ -1196,7 +1205,7 @@ cgx_status cgx_batch_set_config(cgx_batch_plan plan, int64_t item_particles, int
 cgx_status cgx_batch_autotune(cgx_batch_plan plan, void* stream, double* best_ms) {
     if (!plan) return fail(CGX_ERR_INVALID_ARG, "plan is NULL");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const int64_t items[] = {256, 512, 1024, 2048, 4096};
+    const int64_t items[] = {1024, 2048, 4096, 8192, 16384};
     cudaEvent_t e0, e1;
     CGX_CUDA(cudaEventCreate(&e0));
     cudaError_t ce = cudaEventCreate(&e1);
@@ -1209,7 +1218,6 @@ cgx_status cgx_batch_autotune(cgx_batch_plan plan, void* stream, double* best_ms
     int best_ctas = plan->ctas_per_sm;
     cgx_status s = CGX_OK;
     for (int64_t item : items) {
-        if (plan->p2g && item > kChunk) continue;
         for (int c = 1; c <= plan->max_per_sm && s == CGX_OK; ++c) {
             plan->item = item;
             plan->ctas_per_sm = c;

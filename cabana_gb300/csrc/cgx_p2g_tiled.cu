@@ -6,9 +6,9 @@
 // warp's lanes hit one address -- which is exactly what happens when the
 // particles of a warp share a cell:
 //
-//  * A work item is a tile and a contiguous run (<= 2048) of its particles.
-//    A prep pass stages the operator inputs in shared memory with
-//    asynchronous copies and forms, once per particle, the stencil base node
+//  * A work item is a tile and a contiguous run (<= 16384) of its particles,
+//    taken 2048 at a time. A prep pass stages the operator inputs in shared
+//    memory with asynchronous copies and forms, once per particle, the stencil base node
 //    inside the tile's node box and the FP32 in-cell offsets (one double FMA
 //    per dimension plus integer operations). It then lists the runs of
 //    particles sharing a base node.
@@ -19,15 +19,15 @@
 //    in registers. The CTA's 16 warps pull units of work -- (piece, group)
 //    and then (window, group) -- from shared counters.
 //  * Runs of two or more particles are cut into pieces of <= 256 particles
-//    (a dense cell keeps every warp busy). A piece is walked 32 particles at a time, one particle per
-//    lane, each lane adding its particle into its registers; at the end of
+//    (a dense cell keeps every warp busy). A piece is walked 32 particles at
+//    a time, one particle per lane, each lane adding its particle into its registers; at the end of
 //    the piece the warp reduces the registers across lanes with a
 //    transpose-reduction (each lane ends with 1/32 of the sums) and adds them
 //    into the box with compensated shared atomics -- one shared atomic per
 //    node and channel per piece instead of one per particle.
-//  * Particles of short runs (and of stencils outside the box) are packed in
-//    aligned 32-particle windows and added directly, each lane walking its
-//    stencil from a different node so lanes of one cell do not collide;
+//  * Single particles of their cell (and stencils outside the box) are
+//    compacted into a list, taken 32 at a time and added directly, each lane
+//    walking its stencil from a different node so lanes do not collide;
 //    outside the box they go to global memory with bounds checks, so the tile
 //    ordering never changes the result.
 //  * At the end of a work item the box is flushed to the Array, one atomic
@@ -40,7 +40,11 @@ namespace {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kChunk = 2048;        // particles per work item (host builds items of this size)
+constexpr int kChunk = 2048;        // particles staged in shared memory at a time
+// Particles per work item (the host builds items of this size). An item is
+// processed in chunks of kChunk with one node box flush at its end, so dense
+// tiles flush once per kItem particles.
+constexpr int kItem = 16384;
 constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
 constexpr int kSmallRun = 2;        // shorter runs (single particles) add each particle directly
 // Long runs are cut into pieces of at most kPiece particles so that all the
@@ -356,14 +360,13 @@ __device__ __forceinline__ void run_piece(const TiledParams& prm, const TiledGeo
     }
 }
 
-// One aligned 32-particle window wi for channel group gi: each lane whose
-// particle is flagged direct (short run, or stencil outside the box) adds
-// it on its own.
+// One window of the compacted list of particles added directly (single
+// particles of their cell, or stencils outside the box), for channel group
+// gi: each lane adds its item particle i (-1: none) on its own.
 template <int ORDER, int TILE, bool GRAD>
 __device__ __forceinline__ void run_window(const TiledParams& prm, const TiledGeom& geo, float* box_smem,
-                                           const float4* prep, const float* srcs, const unsigned char* direct,
-                                           int wi, const ChanSmem* cs, int gi, const int* origin,
-                                           int64_t item_begin, int lane) {
+                                           const float4* prep, const float* srcs, int i, const ChanSmem* cs, int gi,
+                                           const int* origin, int64_t item_begin, int lane) {
     using SH = P2GShape<ORDER>;
     constexpr int BB = TILE + ORDER;
     constexpr int K = SH::K;
@@ -371,10 +374,9 @@ __device__ __forceinline__ void run_window(const TiledParams& prm, const TiledGe
     const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi);
     const int first = gc.first, count = gc.count;
     {
-        const int i = wi * 32 + lane;
-        const bool active = direct[i] != 0;
+        const bool active = i >= 0;
         float coef[CH][3];
-        gc.load(srcs, i, active, coef);
+        gc.load(srcs, active ? i : 0, active, coef);
         if (!active) return;
         const float4 pu = prep[i];
         const int key = __float_as_int(pu.w);
@@ -411,10 +413,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     __shared__ int item_idx;
     __shared__ int runs[kChunk + 1];
     __shared__ int2 pieces[kMaxPieces];
-    __shared__ unsigned char direct[kChunk];
     __shared__ unsigned char run_direct[kChunk];  // per run: its particles are added directly
-    __shared__ unsigned win_mask[kChunk / 32 / 32 + 1];
-    __shared__ int n_runs, n_big;
+    __shared__ int16_t dlist[kChunk];             // particles added directly, in order
+    __shared__ int n_runs, n_big, n_direct;
     __shared__ int next_run[2 * kMaxGroups];
     __shared__ int warp_sums[kWarps];
     __shared__ TiledGeom sgeo;  // instance of the current work item (batched launches)
@@ -437,9 +438,6 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             item_idx = next_idx;
             next_idx = atomicAdd(prm.work_counter, 1);
         }
-        if (threadIdx.x < 2 * kMaxGroups) next_run[threadIdx.x] = 0;
-        if (threadIdx.x < kChunk / 32 / 32 + 1) win_mask[threadIdx.x] = 0u;
-        if (threadIdx.x == 0) n_big = 0;
         for (int i = threadIdx.x * 4; i < prm.smem_floats; i += blockDim.x * 4) {
             if (i + 3 < prm.smem_floats)
                 *reinterpret_cast<float4*>(box_smem + i) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -458,16 +456,6 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             cur_inst = it.instance;
             __syncthreads();
         }
-        {
-            // Pull the next item's coordinates and operator inputs into L2
-            // while this item is processed: its prep then waits on L2, not HBM.
-            const int64_t nidx = next_idx;
-            if (nidx < nwork) {
-                const WorkItem nx = prm.work[nidx];
-                prefetch_item(BATCHED ? prm.instances + nx.instance : &prm.geom, prm.n_ops, nx.begin, nx.end);
-            }
-        }
-        const int len = int(it.end - it.begin);
         int origin[3];
         {
             const int t2 = it.tile % geo.num_tiles[2];
@@ -477,161 +465,192 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             origin[1] = t1 * prm.tile[1];
             origin[2] = t2 * prm.tile[2];
         }
-        // Sources (raw values; multipliers are applied at use): asynchronous
-        // copies, one component at a time, all in flight together.
-        for (int sidx = 0; sidx < prm.n_sources; ++sidx) {
-            const Source src = prm.sources[sidx];
-            const DField f = geo.x[src.op];
-            float* dst = srcs + sidx * kChunk;
-            if (f.log2vl == 0 && f.dtype == CGX_F32) {
-                const float* base = reinterpret_cast<const float*>(f.data) + int64_t(src.comp) * f.comp_stride +
-                                    it.begin * f.soa_stride;
-                const int64_t stride = f.soa_stride;
-                for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, base + i * stride);
-            } else {
-                for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(geo, src, it.begin + i);
-            }
-        }
-        // Prep: base node key in the box and in-cell offsets of each thread's
-        // kChunk / kThreads consecutive particles (coordinates all loaded
-        // before any is used), then the runs of equal keys.
-        constexpr int PER = kChunk / kThreads;
-        int keys[PER];
-        int rid[PER];  // run index of each of this thread's particles
-        {
-            double xs[PER][3];
-#pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x * PER + q;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(geo.points, it.begin + i, d) : 0.0;
-            }
-#pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x * PER + q;
-                keys[q] = kKeyInvalid;
-                if (i >= len) continue;
-                int s[3];
-                float u[3];
-                if (!form_from<ORDER>(geo, xs[q], s, u)) {
-                    raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
-                } else {
-                    int l[3];
-                    bool inbox = true;
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        l[d] = s[d] - origin[d];
-                        inbox &= (l[d] >= 0) && (l[d] + K <= BB);
-                    }
-                    keys[q] = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
+        // The item is processed in chunks of kChunk particles staged in shared
+        // memory; the node box accumulates over all of them and is flushed once.
+        for (int64_t cb = it.begin; cb < it.end; cb += kChunk) {
+            if (threadIdx.x < 2 * kMaxGroups) next_run[threadIdx.x] = 0;
+            if (threadIdx.x == 0) n_big = 0;
+            const int len = int(it.end - cb < kChunk ? it.end - cb : kChunk);
+            {
+                // Pull the next chunk's coordinates and operator inputs (of
+                // this item, or the first chunk of the next one) into L2 while
+                // this chunk is processed: its prep then waits on L2, not HBM.
+                const int64_t nidx = next_idx;
+                if (cb + kChunk < it.end) {
+                    const int64_t ne = cb + 2 * kChunk < it.end ? cb + 2 * kChunk : it.end;
+                    prefetch_item(&geo, prm.n_ops, cb + kChunk, ne);
+                } else if (nidx < nwork) {
+                    const WorkItem nx = prm.work[nidx];
+                    const int64_t ne = nx.begin + kChunk < nx.end ? nx.begin + kChunk : nx.end;
+                    prefetch_item(BATCHED ? prm.instances + nx.instance : &prm.geom, prm.n_ops, nx.begin, ne);
                 }
-                prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(keys[q]));
             }
-        }
-        cp_async_wait_all();
-        __syncthreads();
-        // Run starts: particle i starts a run when its key differs from i-1.
-        {
-            int flags = 0, nstart = 0;
+            // Sources (raw values; multipliers are applied at use): asynchronous
+            // copies, one component at a time, all in flight together.
+            for (int sidx = 0; sidx < prm.n_sources; ++sidx) {
+                const Source src = prm.sources[sidx];
+                const DField f = geo.x[src.op];
+                float* dst = srcs + sidx * kChunk;
+                if (f.log2vl == 0 && f.dtype == CGX_F32) {
+                    const float* base = reinterpret_cast<const float*>(f.data) + int64_t(src.comp) * f.comp_stride +
+                                        cb * f.soa_stride;
+                    const int64_t stride = f.soa_stride;
+                    for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, base + i * stride);
+                } else {
+                    for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(geo, src, cb + i);
+                }
+            }
+            // Prep: base node key in the box and in-cell offsets of each thread's
+            // kChunk / kThreads consecutive particles (coordinates all loaded
+            // before any is used), then the runs of equal keys.
+            constexpr int PER = kChunk / kThreads;
+            int keys[PER];
+            int rid[PER];  // run index of each of this thread's particles
+            {
+                double xs[PER][3];
 #pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x * PER + q;
-                int prev = kKeyInvalid - 1;
-                if (i > 0) prev = q == 0 ? __float_as_int(prep[i - 1].w) : keys[q - 1];
-                const bool st = i < len && keys[q] != prev;
-                flags |= st ? (1 << q) : 0;
-                nstart += st ? 1 : 0;
-            }
-            // block exclusive scan of nstart
-            int x = nstart;
+                for (int q = 0; q < PER; ++q) {
+                    const int i = threadIdx.x * PER + q;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
+                    for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(geo.points, cb + i, d) : 0.0;
+                }
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const int i = threadIdx.x * PER + q;
+                    keys[q] = kKeyInvalid;
+                    if (i >= len) continue;
+                    int s[3];
+                    float u[3];
+                    if (!form_from<ORDER>(geo, xs[q], s, u)) {
+                        raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+                    } else {
+                        int l[3];
+                        bool inbox = true;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            l[d] = s[d] - origin[d];
+                            inbox &= (l[d] >= 0) && (l[d] + K <= BB);
+                        }
+                        keys[q] = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
+                    }
+                    prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(keys[q]));
+                }
             }
-            if (lane == 31) warp_sums[warp] = x;
+            cp_async_wait_all();
             __syncthreads();
-            int wp = 0;
-            for (int w2 = 0; w2 < warp; ++w2) wp += warp_sums[w2];
-            int pos = wp + x - nstart;
+            // Run starts: particle i starts a run when its key differs from i-1.
+            {
+                int flags = 0, nstart = 0;
 #pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                if (flags & (1 << q)) runs[pos++] = threadIdx.x * PER + q;
-                rid[q] = pos - 1;  // run of particle threadIdx.x * PER + q
-            }
-            if (threadIdx.x == kThreads - 1) {
-                n_runs = pos;
-                runs[pos] = len;
-            }
-        }
-        __syncthreads();
-        // Classify runs: long runs inside the box go to the big list, the
-        // particles of the others are added directly, window by window.
-        for (int r = threadIdx.x; r < n_runs; r += blockDim.x) {
-            const int rb = runs[r], re = runs[r + 1];
-            const int key = __float_as_int(prep[rb].w);
-            const bool is_big = key >= 0 && re - rb >= kSmallRun;
-            if (is_big) {
-                // n_big counts pieces: at most kChunk / kPiece + (number of big runs) <= kMaxPieces
-                const int np = (re - rb + kPiece - 1) / kPiece;
-                const int base = atomicAdd(&n_big, np);
-                for (int q = 0; q < np; ++q)
-                    pieces[base + q] = make_int2(rb + q * kPiece, min(re, rb + (q + 1) * kPiece));
-            }
-            run_direct[r] = (!is_big && key != kKeyInvalid) ? 1 : 0;
-        }
-        __syncthreads();
-        // Per-particle direct flags and the windows that hold any, each
-        // thread for its own particles (a run's length never serialises).
-        {
-            bool any = false;
+                for (int q = 0; q < PER; ++q) {
+                    const int i = threadIdx.x * PER + q;
+                    int prev = kKeyInvalid - 1;
+                    if (i > 0) prev = q == 0 ? __float_as_int(prep[i - 1].w) : keys[q - 1];
+                    const bool st = i < len && keys[q] != prev;
+                    flags |= st ? (1 << q) : 0;
+                    nstart += st ? 1 : 0;
+                }
+                // block exclusive scan of nstart
+                int x = nstart;
 #pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x * PER + q;
-                const unsigned char d = i < len ? run_direct[rid[q]] : 0;
-                direct[i] = d;
-                any |= d != 0;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) warp_sums[warp] = x;
+                __syncthreads();
+                int wp = 0;
+                for (int w2 = 0; w2 < warp; ++w2) wp += warp_sums[w2];
+                int pos = wp + x - nstart;
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    if (flags & (1 << q)) runs[pos++] = threadIdx.x * PER + q;
+                    rid[q] = pos - 1;  // run of particle threadIdx.x * PER + q
+                }
+                if (threadIdx.x == kThreads - 1) {
+                    n_runs = pos;
+                    runs[pos] = len;
+                }
             }
-            if (any) {
-                const int wi = (threadIdx.x * PER) >> 5;
-                atomicOr(&win_mask[wi >> 5], 1u << (wi & 31));
+            __syncthreads();
+            // Classify runs: long runs inside the box go to the big list, the
+            // particles of the others are added directly, window by window.
+            for (int r = threadIdx.x; r < n_runs; r += blockDim.x) {
+                const int rb = runs[r], re = runs[r + 1];
+                const int key = __float_as_int(prep[rb].w);
+                const bool is_big = key >= 0 && re - rb >= kSmallRun;
+                if (is_big) {
+                    // n_big counts pieces: at most kChunk / kPiece + (number of big runs) <= kMaxPieces
+                    const int np = (re - rb + kPiece - 1) / kPiece;
+                    const int base = atomicAdd(&n_big, np);
+                    for (int q = 0; q < np; ++q)
+                        pieces[base + q] = make_int2(rb + q * kPiece, min(re, rb + (q + 1) * kPiece));
+                }
+                run_direct[r] = (!is_big && key != kKeyInvalid) ? 1 : 0;
             }
+            __syncthreads();
+            // The particles added directly, compacted into a list (in order)
+            // so their windows are full: each thread flags its own particles
+            // and a block scan places them.
+            {
+                int dflags = 0, nd = 0;
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const int i = threadIdx.x * PER + q;
+                    const bool d = i < len && run_direct[rid[q]] != 0;
+                    dflags |= d ? (1 << q) : 0;
+                    nd += d ? 1 : 0;
+                }
+                int x = nd;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) warp_sums[warp] = x;
+                __syncthreads();
+                int pos = x - nd;
+                for (int w2 = 0; w2 < warp; ++w2) pos += warp_sums[w2];
+#pragma unroll
+                for (int q = 0; q < PER; ++q)
+                    if (dflags & (1 << q)) dlist[pos++] = int16_t(threadIdx.x * PER + q);
+                if (threadIdx.x == kThreads - 1) n_direct = pos;
+            }
+            __syncthreads();
+            {
+                // Units of work are (piece, group) and then (window, group),
+                // pulled by any warp from two shared counters: every warp stays
+                // busy whatever the mix of value and gradient groups.
+                const int nunit = n_big * ng, ndir = n_direct, nwin = (ndir + 31) >> 5;
+                while (true) {
+                    int u = 0;
+                    if (lane == 0) u = atomicAdd(&next_run[0], 1);
+                    u = __shfl_sync(0xffffffffu, u, 0);
+                    if (u >= nunit) break;
+                    const int gi = u % ng;
+                    const int2 piece = pieces[u / ng];
+                    if (prm.groups[gi].gradient)
+                        run_piece<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
+                    else
+                        run_piece<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
+                }
+                const int wunit = nwin * ng;
+                while (true) {
+                    int u = 0;
+                    if (lane == 0) u = atomicAdd(&next_run[1], 1);
+                    u = __shfl_sync(0xffffffffu, u, 0);
+                    if (u >= wunit) break;
+                    const int gi = u % ng, wi = u / ng;
+                    const int k = wi * 32 + lane;
+                    const int i = k < ndir ? int(dlist[k]) : -1;  // item particle of this lane, or none
+                    if (prm.groups[gi].gradient)
+                        run_window<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, i, cs, gi, origin, cb, lane);
+                    else
+                        run_window<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, i, cs, gi, origin, cb, lane);
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        {
-            // Units of work are (piece, group) and then (window, group),
-            // pulled by any warp from two shared counters: every warp stays
-            // busy whatever the mix of value and gradient groups.
-            const int nunit = n_big * ng, nwin = (len + 31) >> 5;
-            while (true) {
-                int u = 0;
-                if (lane == 0) u = atomicAdd(&next_run[0], 1);
-                u = __shfl_sync(0xffffffffu, u, 0);
-                if (u >= nunit) break;
-                const int gi = u % ng;
-                const int2 piece = pieces[u / ng];
-                if (prm.groups[gi].gradient)
-                    run_piece<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
-                else
-                    run_piece<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
-            }
-            const int wunit = nwin * ng;
-            while (true) {
-                int u = 0;
-                if (lane == 0) u = atomicAdd(&next_run[1], 1);
-                u = __shfl_sync(0xffffffffu, u, 0);
-                if (u >= wunit) break;
-                const int gi = u % ng, wi = u / ng;
-                if (!(win_mask[wi >> 5] & (1u << (wi & 31)))) continue;
-                if (prm.groups[gi].gradient)
-                    run_window<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, direct, wi, cs, gi, origin, it.begin,
-                                                  lane);
-                else
-                    run_window<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, direct, wi, cs, gi, origin,
-                                                   it.begin, lane);
-            }
-        }
-        __syncthreads();
         // Flush the box: one atomic per touched node and dof.
         for (int slot = 0; slot < prm.n_arrays; ++slot) {
             const TiledArray& ta = prm.arrays[slot];
@@ -709,7 +728,7 @@ int p2g_group_capacity(int order, bool gradient) {
     return 0;
 }
 
-int64_t p2g_tiled_chunk() { return kChunk; }
+int64_t p2g_tiled_chunk() { return kItem; }
 
 size_t p2g_tiled_smem(const TiledParams& prm, size_t box_bytes) { return smem_bytes(prm, box_bytes); }
 

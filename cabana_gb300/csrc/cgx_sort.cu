@@ -259,15 +259,32 @@ __global__ void key_hist_kernel(const int32_t* keys, int64_t begin, int64_t end,
     }
 }
 
+// One thread per element: neighbouring lanes move the components of one
+// particle, so the gathers read whole particles and the scratch copy is
+// written and read contiguously. The element -> (particle, component) split
+// uses 32-bit division whenever the element count allows it.
+__device__ __forceinline__ void split_element(int64_t e, int ncomp, bool small, int64_t& i, int& c) {
+    if (small) {
+        const uint32_t q = uint32_t(e) / uint32_t(ncomp);
+        i = q;
+        c = int(uint32_t(e) - q * uint32_t(ncomp));
+    } else {
+        i = e / ncomp;
+        c = int(e - i * ncomp);
+    }
+}
+
 template <class T>
 __global__ void permute_gather_kernel(const uint64_t* perm, int64_t begin, int64_t end, DField f, int ncomp,
                                       T* scratch) {
     const int64_t total = (end - begin) * ncomp;
+    const bool small = total < (int64_t(1) << 32);
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     const T* data = reinterpret_cast<const T*>(f.data);
     for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int64_t i = e / ncomp;
-        const int c = int(e - i * ncomp);
+        int64_t i;
+        int c;
+        split_element(e, ncomp, small, i, c);
         scratch[e] = data[field_offset(f, int64_t(perm[i]), c)];
     }
 }
@@ -275,11 +292,13 @@ __global__ void permute_gather_kernel(const uint64_t* perm, int64_t begin, int64
 template <class T>
 __global__ void permute_copy_back_kernel(int64_t begin, int64_t end, DField f, int ncomp, const T* scratch) {
     const int64_t total = (end - begin) * ncomp;
+    const bool small = total < (int64_t(1) << 32);
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     T* data = reinterpret_cast<T*>(f.data);
     for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int64_t i = e / ncomp;
-        const int c = int(e - i * ncomp);
+        int64_t i;
+        int c;
+        split_element(e, ncomp, small, i, c);
         data[field_offset(f, begin + i, c)] = scratch[e];
     }
 }

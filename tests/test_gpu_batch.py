@@ -158,7 +158,7 @@ def test_batch_autotune():
         best = plan.autotune()
         assert best > 0.0
         item, ctas = plan.config()
-        assert item in (256, 512, 1024, 2048, 4096) and ctas >= 1
+        assert item in (1024, 2048, 4096, 8192, 16384) and ctas >= 1
     pp.set_config(512, 1)
     assert pp.config() == (512, 1)
     _zero(batch)
