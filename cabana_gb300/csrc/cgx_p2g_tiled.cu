@@ -8,9 +8,9 @@
 //
 //  * A work item is a tile and a contiguous run (<= 16384) of its particles,
 //    taken 2048 at a time. A prep pass stages the operator inputs in shared
-//    memory with asynchronous copies and forms, once per particle, the stencil base node
-//    inside the tile's node box and the FP32 in-cell offsets (one double FMA
-//    per dimension plus integer operations). It then lists the runs of
+//    memory with asynchronous copies and forms, once per particle, the
+//    stencil base node inside the tile's node box and the FP32 in-cell
+//    offsets (integer operations only, fixed_logical). It then lists the runs of
 //    particles sharing a base node.
 //  * Operators are lowered to channels: one grid dof that receives, per
 //    point, a * W (value channel) or b . grad W (gradient channel). Channels
@@ -51,6 +51,10 @@ constexpr int kSmallRun = 2;        // shorter runs (single particles) add each 
 // warps of a channel group share a dense cell, each piece reduced on its own.
 constexpr int kPiece = 256;
 constexpr int kMaxPieces = kChunk / kSmallRun + kChunk / kPiece + 1;
+// Extra floats per operator staging region: a dense field block is copied
+// from the 16-byte boundary below its first element (up to 3 floats early)
+// and rounded up to whole 16-byte copies (up to 3 floats late).
+constexpr int kOpSlack = 8;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
 
@@ -109,9 +113,8 @@ __device__ __forceinline__ bool form_from(const TiledGeom& geo, const double* x,
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(x[d], geo.mesh.rdx[d], geo.c0[d]);
         int c;
-        ok &= split_logical(t, c, u[d]);
+        ok &= fixed_logical(x[d], geo.fx[d], c, u[d]);
         s[d] = c + first_offset(ORDER);
         ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
@@ -123,9 +126,8 @@ __device__ __forceinline__ bool form_point(const TiledGeom& geo, int64_t p, int*
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(load_field<double>(geo.points, p, d), geo.mesh.rdx[d], geo.c0[d]);
         int c;
-        ok &= split_logical(t, c, u[d]);
+        ok &= fixed_logical(load_field<double>(geo.points, p, d), geo.fx[d], c, u[d]);
         s[d] = c + first_offset(ORDER);
         ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
@@ -289,13 +291,14 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
 
 // The source rows and multipliers of channel group gi, and the per-lane
 // coefficient load: coef[c][n] = source n of channel c of particle i times
-// its multiplier. srcs[s * kChunk + i] is raw source s of item particle i.
+// its multiplier; raw source s of item particle i is srcs[src_off[s] + i * src_str[s]].
 template <int CH, int NS>
 struct GroupCoef {
     int first, count;
-    int srow[CH][NS];
+    int soff[CH][NS];  // staging offset of each source row (-1: none)
+    int sstr[CH][NS];  // its stride between particles
     float smul[CH][NS];
-    __device__ __forceinline__ GroupCoef(const TiledParams& prm, int gi) {
+    __device__ __forceinline__ GroupCoef(const TiledParams& prm, int gi, const int* src_off, const int* src_str) {
         const ChannelGroup grp = prm.groups[gi];
         first = grp.first;
         count = grp.count;
@@ -303,8 +306,10 @@ struct GroupCoef {
         for (int c = 0; c < CH; ++c)
 #pragma unroll
             for (int n = 0; n < NS; ++n) {
-                srow[c][n] = c < count ? prm.channels[first + c].src[n] : -1;
-                smul[c][n] = srow[c][n] >= 0 ? prm.sources[srow[c][n]].mult : 0.0f;
+                const int rr = c < count ? prm.channels[first + c].src[n] : -1;
+                soff[c][n] = rr >= 0 ? src_off[rr] : -1;
+                sstr[c][n] = rr >= 0 ? src_str[rr] : 0;
+                smul[c][n] = rr >= 0 ? prm.sources[rr].mult : 0.0f;
             }
     }
     __device__ __forceinline__ void load(const float* srcs, int i, bool active, float (*coef)[3]) const {
@@ -312,8 +317,9 @@ struct GroupCoef {
         for (int c = 0; c < CH; ++c)
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
-                const int rr = n < NS ? srow[c][n < NS ? n : 0] : -1;
-                coef[c][n] = (rr >= 0 && active) ? srcs[rr * kChunk + i] * smul[c][n < NS ? n : 0] : 0.0f;
+                const int m = n < NS ? n : 0;
+                const bool has = n < NS && soff[c][m] >= 0;
+                coef[c][n] = (has && active) ? srcs[soff[c][m] + i * sstr[c][m]] * smul[c][m] : 0.0f;
             }
     }
 };
@@ -324,13 +330,13 @@ struct GroupCoef {
 // key) of item particle i.
 template <int ORDER, int TILE, bool GRAD>
 __device__ __forceinline__ void run_piece(const TiledParams& prm, const TiledGeom& geo, float* box_smem,
-                                          const float4* prep, const float* srcs, int2 piece, const ChanSmem* cs,
-                                          int gi, int lane) {
+                                          const float4* prep, const float* srcs, const int* src_off,
+                                          const int* src_str, int2 piece, const ChanSmem* cs, int gi, int lane) {
     using SH = P2GShape<ORDER>;
     constexpr int K = SH::K;
     constexpr int CH = GRAD ? SH::CG : SH::CV;
     constexpr int NPAD = GRAD ? SH::NG : SH::NV;
-    const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi);
+    const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi, src_off, src_str);
     const int first = gc.first, count = gc.count;
     float acc[NPAD];
 #pragma unroll
@@ -365,13 +371,14 @@ __device__ __forceinline__ void run_piece(const TiledParams& prm, const TiledGeo
 // gi: each lane adds its item particle i (-1: none) on its own.
 template <int ORDER, int TILE, bool GRAD>
 __device__ __forceinline__ void run_window(const TiledParams& prm, const TiledGeom& geo, float* box_smem,
-                                           const float4* prep, const float* srcs, int i, const ChanSmem* cs, int gi,
-                                           const int* origin, int64_t item_begin, int lane) {
+                                           const float4* prep, const float* srcs, const int* src_off,
+                                           const int* src_str, int i, const ChanSmem* cs, int gi, const int* origin,
+                                           int64_t item_begin, int lane) {
     using SH = P2GShape<ORDER>;
     constexpr int BB = TILE + ORDER;
     constexpr int K = SH::K;
     constexpr int CH = GRAD ? SH::CG : SH::CV;
-    const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi);
+    const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi, src_off, src_str);
     const int first = gc.first, count = gc.count;
     {
         const bool active = i >= 0;
@@ -429,6 +436,21 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
         cs[c].comp_off = (BB * BB * BB) * ta.a.dofs;
         cs[c].dofs = ta.a.dofs;
     }
+    // Staging regions of the operator inputs: op o owns op_nsrc[o] * kChunk
+    // + kOpSlack floats (16-byte aligned); per chunk, src_off / src_str place
+    // source s of item particle i at srcs[src_off[s] + i * src_str[s]].
+    __shared__ int op_base[kMaxOps], op_nsrc[kMaxOps];
+    __shared__ int src_off[kMaxSources], src_str[kMaxSources];
+    if (threadIdx.x == 0) {
+        int base = 0;
+        for (int o = 0; o < prm.n_ops; ++o) {
+            int n = 0;
+            for (int s = 0; s < prm.n_sources; ++s) n += prm.sources[s].op == o ? 1 : 0;
+            op_base[o] = base;
+            op_nsrc[o] = n;
+            base += n > 0 ? n * kChunk + kOpSlack : 0;
+        }
+    }
     const int ng = prm.n_groups;
     const int64_t nwork = *prm.work_count;
     __shared__ int next_idx;  // the item after the current one (its inputs are prefetched into L2)
@@ -485,19 +507,48 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     prefetch_item(BATCHED ? prm.instances + nx.instance : &prm.geom, prm.n_ops, nx.begin, ne);
                 }
             }
-            // Sources (raw values; multipliers are applied at use): asynchronous
-            // copies, one component at a time, all in flight together.
-            for (int sidx = 0; sidx < prm.n_sources; ++sidx) {
-                const Source src = prm.sources[sidx];
-                const DField f = geo.x[src.op];
-                float* dst = srcs + sidx * kChunk;
-                if (f.log2vl == 0 && f.dtype == CGX_F32) {
-                    const float* base = reinterpret_cast<const float*>(f.data) + int64_t(src.comp) * f.comp_stride +
-                                        cb * f.soa_stride;
-                    const int64_t stride = f.soa_stride;
-                    for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, base + i * stride);
+            // Sources (raw values; multipliers are applied at use), as
+            // asynchronous copies all in flight together. A dense FP32 field
+            // whose components are all sources is copied as one block of
+            // 16-byte copies from the 16-byte boundary at or below its first
+            // element (its components are then read with the field's stride);
+            // other fields one component at a time.
+            for (int o = 0; o < prm.n_ops; ++o) {
+                const int nsrc = op_nsrc[o];
+                if (nsrc == 0) continue;
+                const DField f = geo.x[o];
+                float* region = srcs + op_base[o];
+                const bool dense = f.log2vl == 0 && f.comp_stride == 1 && f.dtype == CGX_F32 && f.soa_stride == nsrc;
+                if (dense) {
+                    const float* first = reinterpret_cast<const float*>(f.data) + cb * f.soa_stride;
+                    const int shift = int((reinterpret_cast<uintptr_t>(first) & 15) >> 2);
+                    const float* a0 = first - shift;  // same 16-byte block as the first element
+                    const int nvec = (shift + len * nsrc + 3) >> 2;
+                    for (int v = threadIdx.x; v < nvec; v += blockDim.x) cp_async16(region + 4 * v, a0 + 4 * v);
+                    if (threadIdx.x < prm.n_sources && prm.sources[threadIdx.x].op == o) {
+                        src_off[threadIdx.x] = op_base[o] + shift + prm.sources[threadIdx.x].comp;
+                        src_str[threadIdx.x] = nsrc;
+                    }
                 } else {
-                    for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(geo, src, cb + i);
+                    int j = 0;
+                    for (int s = 0; s < prm.n_sources; ++s) {
+                        const Source src = prm.sources[s];
+                        if (src.op != o) continue;
+                        float* dst = region + j * kChunk;
+                        if (threadIdx.x == 0) {
+                            src_off[s] = op_base[o] + j * kChunk;
+                            src_str[s] = 1;
+                        }
+                        ++j;
+                        if (f.log2vl == 0 && f.dtype == CGX_F32) {
+                            const float* base = reinterpret_cast<const float*>(f.data) +
+                                                int64_t(src.comp) * f.comp_stride + cb * f.soa_stride;
+                            const int64_t stride = f.soa_stride;
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, base + i * stride);
+                        } else {
+                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(geo, src, cb + i);
+                        }
+                    }
                 }
             }
             // Prep: base node key in the box and in-cell offsets of each thread's
@@ -630,9 +681,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     const int gi = u % ng;
                     const int2 piece = pieces[u / ng];
                     if (prm.groups[gi].gradient)
-                        run_piece<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
+                        run_piece<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, src_off, src_str, piece, cs, gi, lane);
                     else
-                        run_piece<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, piece, cs, gi, lane);
+                        run_piece<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, src_off, src_str, piece, cs, gi, lane);
                 }
                 const int wunit = nwin * ng;
                 while (true) {
@@ -644,9 +695,11 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     const int k = wi * 32 + lane;
                     const int i = k < ndir ? int(dlist[k]) : -1;  // item particle of this lane, or none
                     if (prm.groups[gi].gradient)
-                        run_window<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, i, cs, gi, origin, cb, lane);
+                        run_window<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, src_off, src_str, i, cs, gi, origin, cb,
+                                                      lane);
                     else
-                        run_window<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, i, cs, gi, origin, cb, lane);
+                        run_window<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, src_off, src_str, i, cs, gi, origin, cb,
+                                                      lane);
                 }
             }
             __syncthreads();
@@ -677,7 +730,8 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
 }
 
 size_t smem_bytes(const TiledParams& prm, size_t box_bytes) {
-    return (box_bytes + 15) / 16 * 16 + size_t(kChunk) * sizeof(float4) + size_t(prm.n_sources) * kChunk * sizeof(float);
+    return (box_bytes + 15) / 16 * 16 + size_t(kChunk) * sizeof(float4) +
+           (size_t(prm.n_sources) * kChunk + size_t(prm.n_ops) * kOpSlack) * sizeof(float);
 }
 
 template <int ORDER, bool BATCHED>
