@@ -391,14 +391,19 @@ bool setup_tiled(TiledParams& prm, const cgx_op* ops, int n_ops, int spline_orde
     return ok;
 }
 
-// The mesh and buffers of one instance, with the slots of `prm`.
-void fill_geom(TiledGeom& g, const TiledParams& prm, const cgx_mesh& mesh, const cgx_field& points, const cgx_op* ops,
+// The mesh and buffers of one instance, with the slots of `prm`. Returns
+// false when the mesh is beyond the integer mapping of the tiled kernels
+// (origin more than 2^28 cells from zero, or extents of 2^28 nodes).
+bool fill_geom(TiledGeom& g, const TiledParams& prm, const cgx_mesh& mesh, const cgx_field& points, const cgx_op* ops,
                int n_ops, const cgx_tiling& tiling, int spline_order) {
     std::memset(&g, 0, sizeof(g));
     g.mesh = to_dmesh(mesh);
     const int shift_even = (spline_order % 2 == 0) ? 1 : 0;
+    bool ok = true;
     for (int d = 0; d < 3; ++d) {
         g.c0[d] = -g.mesh.low[d] * g.mesh.rdx[d] + 0.5 * shift_even;
+        g.fx[d] = fixed_map(g.mesh.rdx[d], g.c0[d]);
+        ok &= fixed_map_ok(g.c0[d]) && g.mesh.ext[d] < (1 << 28);
         g.num_tiles[d] = tiling.num_tiles[d];
     }
     g.points = to_dfield(points);
@@ -409,6 +414,7 @@ void fill_geom(TiledGeom& g, const TiledParams& prm, const cgx_mesh& mesh, const
         a.dtype = ops[o].array.dtype;
         a.dofs = ops[o].array.dofs;
     }
+    return ok;
 }
 
 cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point,
@@ -445,7 +451,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
     if (tiled) {
         TiledParams prm;
         tiled = setup_tiled(prm, ops, n_ops, spline_order, p2g);
-        fill_geom(prm.geom, prm, *mesh, *points, ops, n_ops, *tiling, spline_order);
+        tiled &= fill_geom(prm.geom, prm, *mesh, *points, ops, n_ops, *tiling, spline_order);
         prm.num_point = num_point;
         const int n_arrays = prm.n_arrays;
         const size_t smem = size_t(prm.smem_floats) * sizeof(float);
@@ -1109,7 +1115,10 @@ cgx_status cgx_batch_plan_create(cgx_handle h, const cgx_instance* inst, int n_i
             }
             b->arrays[size_t(i) * n_arrays + slot] = io[o].array;
         }
-        fill_geom(geoms[i], b->prm, inst[i].mesh, inst[i].points, io, n_ops, inst[i].tiling, spline_order);
+        if (!fill_geom(geoms[i], b->prm, inst[i].mesh, inst[i].points, io, n_ops, inst[i].tiling, spline_order)) {
+            delete b;
+            return fail(CGX_ERR_NOT_SUPPORTED, "an instance's mesh origin or extent is beyond the tiled kernels' range");
+        }
         b->meshes[i] = inst[i].mesh;
         b->any_periodic |= ::any_periodic(inst[i].mesh);
         offs[i] = inst[i].tiling.tile_offsets;

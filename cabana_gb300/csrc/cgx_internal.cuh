@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include "../../include/cgx.h"
 
 namespace cgx {
@@ -75,6 +77,12 @@ __device__ __forceinline__ T load_field(const DField& f, int64_t p, int c) {
 __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+// Asynchronous 16-byte global -> shared copy (both addresses 16-byte aligned).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
 }
 
 __device__ __forceinline__ void cp_async_wait_all() {
@@ -315,6 +323,67 @@ __device__ __forceinline__ bool split_logical(double t, int& cell, float& u) {
         ufx = sh >= 32 ? static_cast<unsigned int>(fr >> (sh - 32)) : static_cast<unsigned int>(fr << (32 - sh));
     }
     u = __uint2float_rz(ufx) * 2.3283064365386963e-10f;  // * 2^-32
+    return true;
+}
+
+// The mapping t = x * rdx + c0 of one dimension in integer form, for the
+// FP32 kernels: rdx = r * 2^e with r a 64-bit integer (its leading bit set)
+// and c = c0 * 2^32 rounded to an integer (see fixed_map).
+struct FixedMap {
+    uint64_t r;
+    int64_t c;
+    int32_t e;
+    int32_t reserved;
+};
+
+// Host side: the FixedMap of rdx and c0. Valid for |c0| < 2^28 (the caller
+// checks fixed_map_ok): then every t in [0, 2^29) has |x * rdx| < 2^30 and
+// the 32.32 sum cannot overflow.
+inline FixedMap fixed_map(double rdx, double c0) {
+    FixedMap f;
+    int k = 0;
+    const double m = frexp(rdx, &k);  // rdx = m * 2^k, m in [0.5, 1)
+    f.r = static_cast<uint64_t>(ldexp(m, 64));
+    f.e = k - 64;
+    f.c = static_cast<int64_t>(llround(ldexp(c0, 32)));
+    f.reserved = 0;
+    return f;
+}
+
+inline bool fixed_map_ok(double c0) { return std::fabs(c0) < 268435456.0; }
+
+// Cell index and in-cell offset of t = x * rdx + c0 with integer
+// operations only (no double-precision arithmetic, which runs at 1/64 of the
+// FP32 rate on this part): x = m * 2^(ex - 1075), so x * rdx * 2^32 is the
+// high half of (m * 2^11) * r, shifted by ex + e - 990, then c is added in
+// 32.32 fixed point. The offset keeps 32 fraction bits and is truncated to
+// FP32 toward zero (always < 1). The integer part of x * rdx * 2^32 is
+// exact up to the truncation of the product (t is rounded differently from
+// a double evaluation only in its last bits). Returns false for t < 0,
+// t >= 2^30, infinities and NaN.
+__device__ __forceinline__ bool fixed_logical(double x, const FixedMap& f, int& cell, float& u) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const int ex = int((b >> 52) & 0x7FF);
+    long long t1 = 0;
+    cell = 0;
+    u = 0.0f;
+    if (ex == 0x7FF) return false;  // infinity or NaN
+    if (ex != 0) {                  // zero and subnormals map to 0
+        const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+        const unsigned long long p = __umul64hi(m << 11, f.r);
+        const int sh = ex + f.e - 990;
+        if (sh >= 0) {
+            if (sh > 62 || (p >> (62 - sh)) != 0) return false;  // |x * rdx| >= 2^30
+            t1 = static_cast<long long>(p << sh);
+        } else {
+            t1 = sh < -63 ? 0 : static_cast<long long>(p >> (-sh));
+        }
+        if (b >> 63) t1 = -t1;
+    }
+    const long long t = t1 + f.c;
+    if (t < 0 || t >= (1ll << 62)) return false;
+    cell = int(t >> 32);
+    u = __uint2float_rz(static_cast<unsigned int>(t & 0xFFFFFFFFll)) * 2.3283064365386963e-10f;  // * 2^-32
     return true;
 }
 

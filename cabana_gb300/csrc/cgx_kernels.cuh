@@ -84,7 +84,8 @@ constexpr int kMaxGroups = 16;
 // TiledParams::instances.
 struct TiledGeom {
     DMesh mesh;
-    double c0[3];  // -low * rdx + (0.5 for even orders): t = fma(x, rdx, c0)
+    double c0[3];  // -low * rdx + (0.5 for even orders): t = x * rdx + c0
+    FixedMap fx[3];  // the same mapping in integer form (fixed_logical)
     int32_t num_tiles[3];
     int32_t reserved;
     DField points;

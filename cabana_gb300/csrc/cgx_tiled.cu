@@ -5,8 +5,8 @@
 // sub-runs of up to 1024 particles, so that global memory is touched only in
 // long runs of independent loads and stores:
 //   1. load: the coordinates are read and turned into the stencil base node
-//      inside the tile's node box and FP32 in-cell offsets (one double FMA per
-//      dimension plus integer operations); the current values of the point
+//      inside the tile's node box and FP32 in-cell offsets (integer
+//      operations only, fixed_logical); the current values of the point
 //      fields being accumulated are copied into shared memory;
 //   2. compute: each thread gathers for one particle from the node box staged
 //      in shared memory. All operators that read the array share one pass
@@ -51,9 +51,8 @@ __device__ __forceinline__ bool form_from(const TiledGeom& geo, const double* x,
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(x[d], geo.mesh.rdx[d], geo.c0[d]);
         int c;
-        ok &= split_logical(t, c, u[d]);
+        ok &= fixed_logical(x[d], geo.fx[d], c, u[d]);
         s[d] = c + first_offset(ORDER);
         ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
@@ -65,9 +64,8 @@ __device__ __forceinline__ bool form_point(const TiledGeom& geo, int64_t p, int*
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double t = fma(load_field<double>(geo.points, p, d), geo.mesh.rdx[d], geo.c0[d]);
         int c;
-        ok &= split_logical(t, c, u[d]);
+        ok &= fixed_logical(load_field<double>(geo.points, p, d), geo.fx[d], c, u[d]);
         s[d] = c + first_offset(ORDER);
         ok &= (s[d] >= 0) && (s[d] + ORDER + 1 <= geo.mesh.ext[d]);
     }
