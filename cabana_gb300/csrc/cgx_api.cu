@@ -188,6 +188,8 @@ cgx_status finish_check(cgx_context* h, unsigned flags, cudaStream_t st) {
     if (host_flag & (1 << CGX_ERR_OUT_OF_BOUNDS))
         return fail(CGX_ERR_OUT_OF_BOUNDS, "a point's stencil left the ghosted index space; it was skipped");
     if (host_flag & (1 << CGX_ERR_INVALID_ARG)) return fail(CGX_ERR_INVALID_ARG, "a key was outside [0, nbin)");
+    if (host_flag & (1 << CGX_ERR_TIMEOUT))
+        return fail(CGX_ERR_TIMEOUT, "a bounded device wait gave up; the results are incomplete");
     return CGX_OK;
 }
 

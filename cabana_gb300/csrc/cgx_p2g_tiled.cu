@@ -55,6 +55,9 @@ constexpr int kMaxPieces = kChunk / kSmallRun + kChunk / kPiece + 1;
 // from the 16-byte boundary below its first element (up to 3 floats early)
 // and rounded up to whole 16-byte copies (up to 3 floats late).
 constexpr int kOpSlack = 8;
+// Polls of the bulk-copy barrier before the CTA gives up (CGX_ERR_TIMEOUT);
+// far beyond any copy's latency.
+constexpr int kMaxPolls = 1 << 22;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
 
@@ -441,7 +444,14 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     // source s of item particle i at srcs[src_off[s] + i * src_str[s]].
     __shared__ int op_base[kMaxOps], op_nsrc[kMaxOps];
     __shared__ int src_off[kMaxSources], src_str[kMaxSources];
+    // Dense field blocks arrive by bulk copies completing one phase of
+    // src_bar per chunk; a wait that runs out sets `aborted` for the CTA.
+    __shared__ uint64_t src_bar;
+    __shared__ int aborted;
+    unsigned src_phase = 0;
     if (threadIdx.x == 0) {
+        mbar_init(&src_bar);
+        aborted = 0;
         int base = 0;
         for (int o = 0; o < prm.n_ops; ++o) {
             int n = 0;
@@ -509,10 +519,11 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             }
             // Sources (raw values; multipliers are applied at use), as
             // asynchronous copies all in flight together. A dense FP32 field
-            // whose components are all sources is copied as one block of
-            // 16-byte copies from the 16-byte boundary at or below its first
+            // whose components are all sources is one bulk (TMA) copy, issued
+            // by one thread, from the 16-byte boundary at or below its first
             // element (its components are then read with the field's stride);
-            // other fields one component at a time.
+            // other fields are copied one component at a time.
+            bool bulk = false;  // the same in every thread
             for (int o = 0; o < prm.n_ops; ++o) {
                 const int nsrc = op_nsrc[o];
                 if (nsrc == 0) continue;
@@ -523,8 +534,12 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     const float* first = reinterpret_cast<const float*>(f.data) + cb * f.soa_stride;
                     const int shift = int((reinterpret_cast<uintptr_t>(first) & 15) >> 2);
                     const float* a0 = first - shift;  // same 16-byte block as the first element
-                    const int nvec = (shift + len * nsrc + 3) >> 2;
-                    for (int v = threadIdx.x; v < nvec; v += blockDim.x) cp_async16(region + 4 * v, a0 + 4 * v);
+                    const unsigned bytes = unsigned((shift + len * nsrc + 3) >> 2) * 16u;
+                    if (threadIdx.x == 0) {
+                        mbar_expect_tx(&src_bar, bytes);
+                        bulk_copy_g2s(region, a0, bytes, &src_bar);
+                    }
+                    bulk = true;
                     if (threadIdx.x < prm.n_sources && prm.sources[threadIdx.x].op == o) {
                         src_off[threadIdx.x] = op_base[o] + shift + prm.sources[threadIdx.x].comp;
                         src_str[threadIdx.x] = nsrc;
@@ -551,6 +566,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     }
                 }
             }
+            if (bulk && threadIdx.x == 0) mbar_arrive(&src_bar);
             // Prep: base node key in the box and in-cell offsets of each thread's
             // kChunk / kThreads consecutive particles (coordinates all loaded
             // before any is used), then the runs of equal keys.
@@ -588,7 +604,15 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 }
             }
             cp_async_wait_all();
+            if (bulk) {
+                if (!mbar_wait(&src_bar, src_phase, kMaxPolls)) {
+                    raise_error(prm.error_flag, CGX_ERR_TIMEOUT);
+                    aborted = 1;
+                }
+                src_phase ^= 1u;
+            }
             __syncthreads();
+            if (aborted) break;  // the same in every thread after the barrier
             // Run starts: particle i starts a run when its key differs from i-1.
             {
                 int flags = 0, nstart = 0;
@@ -704,6 +728,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             }
             __syncthreads();
         }
+        if (aborted) break;  // a bulk copy never completed: stop (the error flag is set)
         // Flush the box: one atomic per touched node and dof.
         for (int slot = 0; slot < prm.n_arrays; ++slot) {
             const TiledArray& ta = prm.arrays[slot];
