@@ -107,11 +107,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// Orders this thread's earlier generic-proxy accesses of shared memory
+// before its later bulk copies (asynchronous proxy).
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
 // Bulk global -> shared copy: both addresses 16-byte aligned, bytes a
-// multiple of 16. Orders earlier generic-proxy accesses of shared memory by
-// this thread before the copy's writes.
+// multiple of 16. The caller orders earlier accesses of the destination
+// (fence_proxy_async after the CTA barrier that ends them).
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
                      smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))

@@ -8,7 +8,7 @@
 //
 //  * A work item is a tile and a contiguous run (<= 16384) of its particles,
 //    taken 2048 at a time. A prep pass stages the operator inputs in shared
-//    memory with asynchronous copies and forms, once per particle, the
+//    memory with bulk (TMA) and asynchronous copies and forms, once per particle, the
 //    stencil base node inside the tile's node box and the FP32 in-cell
 //    offsets (integer operations only, fixed_logical). It then lists the runs of
 //    particles sharing a base node.
@@ -443,24 +443,104 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     // + kOpSlack floats (16-byte aligned); per chunk, src_off / src_str place
     // source s of item particle i at srcs[src_off[s] + i * src_str[s]].
     __shared__ int op_base[kMaxOps], op_nsrc[kMaxOps];
+    // Source s is component src_comp[s] of operator src_op[s]'s field, the
+    // src_j[s]-th source of that operator.
+    __shared__ int8_t src_op[kMaxSources], src_comp[kMaxSources], src_j[kMaxSources];
+    // Per operator of the current instance: its FP32 field when the field is
+    // dense (vector length 1, components adjacent and all of them sources),
+    // which is staged by one bulk copy per chunk; null otherwise.
+    __shared__ const float* op_dense[kMaxOps];
     __shared__ int src_off[kMaxSources], src_str[kMaxSources];
     // Dense field blocks arrive by bulk copies completing one phase of
     // src_bar per chunk; a wait that runs out sets `aborted` for the CTA.
     __shared__ uint64_t src_bar;
     __shared__ int aborted;
-    unsigned src_phase = 0;
+    unsigned src_phase = 0u;
     if (threadIdx.x == 0) {
         mbar_init(&src_bar);
         aborted = 0;
         int base = 0;
         for (int o = 0; o < prm.n_ops; ++o) {
             int n = 0;
-            for (int s = 0; s < prm.n_sources; ++s) n += prm.sources[s].op == o ? 1 : 0;
+            for (int s = 0; s < prm.n_sources; ++s) {
+                if (prm.sources[s].op != o) continue;
+                src_op[s] = int8_t(o);
+                src_comp[s] = prm.sources[s].comp;
+                src_j[s] = int8_t(n++);
+            }
             op_base[o] = base;
             op_nsrc[o] = n;
             base += n > 0 ? n * kChunk + kOpSlack : 0;
         }
     }
+    __syncthreads();
+    // Fill op_dense for the instance in `geo` (threads < n_ops; the caller
+    // synchronises before the next stage).
+    auto find_dense = [&]() {
+        if (threadIdx.x < prm.n_ops) {
+            const int o = threadIdx.x, nsrc = op_nsrc[o];
+            const DField f = geo.x[o];
+            const bool dense =
+                nsrc > 0 && f.log2vl == 0 && f.comp_stride == 1 && f.dtype == CGX_F32 && f.soa_stride == nsrc;
+            op_dense[o] = dense ? reinterpret_cast<const float*>(f.data) : nullptr;
+        }
+    };
+    if (!BATCHED) find_dense();  // visible after the first item's barrier
+    // Issue the staging of particles [sb, sb + slen) (raw values; multipliers
+    // are applied at use), all copies in flight together: one bulk copy per
+    // dense field, issued by one thread, from the 16-byte boundary at or below
+    // the first element (components are then read with the field's stride);
+    // component copies for other fields. Returns whether bulk copies were
+    // issued (the same in every thread).
+    auto stage = [&](int64_t sb, int slen) -> bool {
+        if (threadIdx.x < prm.n_sources) {
+            const int s = threadIdx.x, o = src_op[s];
+            const float* dense = op_dense[o];
+            if (dense) {
+                const int shift = int((reinterpret_cast<uintptr_t>(dense + sb * op_nsrc[o]) & 15) >> 2);
+                src_off[s] = op_base[o] + shift + src_comp[s];
+                src_str[s] = op_nsrc[o];
+            } else {
+                src_off[s] = op_base[o] + src_j[s] * kChunk;
+                src_str[s] = 1;
+            }
+        }
+        bool bulk = false;
+        for (int o = 0; o < prm.n_ops; ++o) {
+            const int nsrc = op_nsrc[o];
+            if (nsrc == 0) continue;
+            float* region = srcs + op_base[o];
+            const float* dense = op_dense[o];
+            if (dense) {
+                if (threadIdx.x == 0) {
+                    if (!bulk) fence_proxy_async();  // after the barrier that ended the buffer's last reads
+                    const float* first = dense + sb * nsrc;
+                    const int shift = int((reinterpret_cast<uintptr_t>(first) & 15) >> 2);
+                    const unsigned bytes = unsigned((shift + slen * nsrc + 3) >> 2) * 16u;
+                    mbar_expect_tx(&src_bar, bytes);
+                    bulk_copy_g2s(region, first - shift, bytes, &src_bar);
+                }
+                bulk = true;
+                continue;
+            }
+            const DField f = geo.x[o];
+            for (int s = 0; s < prm.n_sources; ++s) {
+                if (src_op[s] != o) continue;
+                const Source src = prm.sources[s];
+                float* dst = region + src_j[s] * kChunk;
+                if (f.log2vl == 0 && f.dtype == CGX_F32) {
+                    const float* base =
+                        reinterpret_cast<const float*>(f.data) + int64_t(src.comp) * f.comp_stride + sb * f.soa_stride;
+                    const int64_t stride = f.soa_stride;
+                    for (int i = threadIdx.x; i < slen; i += blockDim.x) cp_async4(dst + i, base + i * stride);
+                } else {
+                    for (int i = threadIdx.x; i < slen; i += blockDim.x) dst[i] = load_src(geo, src, sb + i);
+                }
+            }
+        }
+        if (bulk && threadIdx.x == 0) mbar_arrive(&src_bar);
+        return bulk;
+    };
     const int ng = prm.n_groups;
     const int64_t nwork = *prm.work_count;
     __shared__ int next_idx;  // the item after the current one (its inputs are prefetched into L2)
@@ -487,6 +567,8 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             for (int i = threadIdx.x; i < int(sizeof(TiledGeom) / 4); i += blockDim.x) dst[i] = src[i];
             cur_inst = it.instance;
             __syncthreads();
+            find_dense();
+            __syncthreads();
         }
         int origin[3];
         {
@@ -503,6 +585,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             if (threadIdx.x < 2 * kMaxGroups) next_run[threadIdx.x] = 0;
             if (threadIdx.x == 0) n_big = 0;
             const int len = int(it.end - cb < kChunk ? it.end - cb : kChunk);
+            const bool bulk = stage(cb, len);
             {
                 // Pull the next chunk's coordinates and operator inputs (of
                 // this item, or the first chunk of the next one) into L2 while
@@ -517,56 +600,6 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     prefetch_item(BATCHED ? prm.instances + nx.instance : &prm.geom, prm.n_ops, nx.begin, ne);
                 }
             }
-            // Sources (raw values; multipliers are applied at use), as
-            // asynchronous copies all in flight together. A dense FP32 field
-            // whose components are all sources is one bulk (TMA) copy, issued
-            // by one thread, from the 16-byte boundary at or below its first
-            // element (its components are then read with the field's stride);
-            // other fields are copied one component at a time.
-            bool bulk = false;  // the same in every thread
-            for (int o = 0; o < prm.n_ops; ++o) {
-                const int nsrc = op_nsrc[o];
-                if (nsrc == 0) continue;
-                const DField f = geo.x[o];
-                float* region = srcs + op_base[o];
-                const bool dense = f.log2vl == 0 && f.comp_stride == 1 && f.dtype == CGX_F32 && f.soa_stride == nsrc;
-                if (dense) {
-                    const float* first = reinterpret_cast<const float*>(f.data) + cb * f.soa_stride;
-                    const int shift = int((reinterpret_cast<uintptr_t>(first) & 15) >> 2);
-                    const float* a0 = first - shift;  // same 16-byte block as the first element
-                    const unsigned bytes = unsigned((shift + len * nsrc + 3) >> 2) * 16u;
-                    if (threadIdx.x == 0) {
-                        mbar_expect_tx(&src_bar, bytes);
-                        bulk_copy_g2s(region, a0, bytes, &src_bar);
-                    }
-                    bulk = true;
-                    if (threadIdx.x < prm.n_sources && prm.sources[threadIdx.x].op == o) {
-                        src_off[threadIdx.x] = op_base[o] + shift + prm.sources[threadIdx.x].comp;
-                        src_str[threadIdx.x] = nsrc;
-                    }
-                } else {
-                    int j = 0;
-                    for (int s = 0; s < prm.n_sources; ++s) {
-                        const Source src = prm.sources[s];
-                        if (src.op != o) continue;
-                        float* dst = region + j * kChunk;
-                        if (threadIdx.x == 0) {
-                            src_off[s] = op_base[o] + j * kChunk;
-                            src_str[s] = 1;
-                        }
-                        ++j;
-                        if (f.log2vl == 0 && f.dtype == CGX_F32) {
-                            const float* base = reinterpret_cast<const float*>(f.data) +
-                                                int64_t(src.comp) * f.comp_stride + cb * f.soa_stride;
-                            const int64_t stride = f.soa_stride;
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, base + i * stride);
-                        } else {
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_src(geo, src, cb + i);
-                        }
-                    }
-                }
-            }
-            if (bulk && threadIdx.x == 0) mbar_arrive(&src_bar);
             // Prep: base node key in the box and in-cell offsets of each thread's
             // kChunk / kThreads consecutive particles (coordinates all loaded
             // before any is used), then the runs of equal keys.
