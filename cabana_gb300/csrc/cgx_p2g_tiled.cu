@@ -600,9 +600,11 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     prefetch_item(BATCHED ? prm.instances + nx.instance : &prm.geom, prm.n_ops, nx.begin, ne);
                 }
             }
-            // Prep: base node key in the box and in-cell offsets of each thread's
-            // kChunk / kThreads consecutive particles (coordinates all loaded
-            // before any is used), then the runs of equal keys.
+            // Prep: base node key in the box and in-cell offsets of particles
+            // threadIdx.x + q * kThreads (so a warp's coordinate loads cover
+            // adjacent particles; all loaded before any is used). The run scan
+            // below then takes each thread's kChunk / kThreads consecutive
+            // particles.
             constexpr int PER = kChunk / kThreads;
             int keys[PER];
             int rid[PER];  // run index of each of this thread's particles
@@ -610,15 +612,15 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 double xs[PER][3];
 #pragma unroll
                 for (int q = 0; q < PER; ++q) {
-                    const int i = threadIdx.x * PER + q;
+                    const int i = threadIdx.x + q * kThreads;
 #pragma unroll
                     for (int d = 0; d < 3; ++d) xs[q][d] = i < len ? load_field<double>(geo.points, cb + i, d) : 0.0;
                 }
 #pragma unroll
                 for (int q = 0; q < PER; ++q) {
-                    const int i = threadIdx.x * PER + q;
-                    keys[q] = kKeyInvalid;
+                    const int i = threadIdx.x + q * kThreads;
                     if (i >= len) continue;
+                    int key = kKeyInvalid;
                     int s[3];
                     float u[3];
                     if (!form_from<ORDER>(geo, xs[q], s, u)) {
@@ -631,9 +633,9 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                             l[d] = s[d] - origin[d];
                             inbox &= (l[d] >= 0) && (l[d] + K <= BB);
                         }
-                        keys[q] = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
+                        key = inbox ? (l[0] * BB + l[1]) * BB + l[2] : kKeyOutside;
                     }
-                    prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(keys[q]));
+                    prep[i] = make_float4(u[0], u[1], u[2], __int_as_float(key));
                 }
             }
             cp_async_wait_all();
@@ -646,6 +648,11 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             }
             __syncthreads();
             if (aborted) break;  // the same in every thread after the barrier
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int i = threadIdx.x * PER + q;
+                keys[q] = i < len ? __float_as_int(prep[i].w) : kKeyInvalid;
+            }
             // Run starts: particle i starts a run when its key differs from i-1.
             {
                 int flags = 0, nstart = 0;
