@@ -121,6 +121,33 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
                  : "memory");
 }
 
+// Bulk shared -> global copy: both addresses 16-byte aligned, bytes a
+// multiple of 16, tracked by the issuing thread's bulk async-group. The
+// threads that wrote the source order their writes first (fence_proxy_async,
+// then a CTA barrier).
+__device__ __forceinline__ void bulk_copy_s2g(void* dst, const void* src, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+
+// Wait until this thread's bulk stores have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+
+// Wait until this thread's bulk stores are complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
+// Extra floats per staging region of a point field: a dense field block is
+// copied from the 16-byte boundary at or below its first element (up to 3
+// floats early) and rounded up to whole 16-byte copies (up to 3 floats late).
+constexpr int kOpSlack = 8;
+
+// Polls of a bulk-copy barrier before a CTA gives up (CGX_ERR_TIMEOUT); far
+// beyond any copy's latency.
+constexpr int kMaxPolls = 1 << 22;
+
 // Bounded wait for the phase of the given parity to complete. Returns false
 // after `max_tries` polls (the caller records a timeout and stops).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int max_tries) {

@@ -51,13 +51,6 @@ constexpr int kSmallRun = 2;        // shorter runs (single particles) add each 
 // warps of a channel group share a dense cell, each piece reduced on its own.
 constexpr int kPiece = 256;
 constexpr int kMaxPieces = kChunk / kSmallRun + kChunk / kPiece + 1;
-// Extra floats per operator staging region: a dense field block is copied
-// from the 16-byte boundary below its first element (up to 3 floats early)
-// and rounded up to whole 16-byte copies (up to 3 floats late).
-constexpr int kOpSlack = 8;
-// Polls of the bulk-copy barrier before the CTA gives up (CGX_ERR_TIMEOUT);
-// far beyond any copy's latency.
-constexpr int kMaxPolls = 1 << 22;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
 

@@ -142,49 +142,53 @@ __device__ __forceinline__ void gather_sums(const TiledGeom& geo, const DArray& 
     }
 }
 
+// Where a pass stages the point-field values of operator o: component c of
+// pass particle i is out[base[o] + i * pstr[o] + c * cstr[o]] (base -1: the
+// operator reads another array).
+struct OutMap {
+    int base[kMaxOps];
+    int pstr[kMaxOps];
+    int cstr[kMaxOps];
+};
+
 // Adds multiplier * result of every operator of this launch into the staged
-// point-field values (out[col * kSub + i]).
+// point-field values.
 template <int NDOF>
-__device__ __forceinline__ void apply_ops(const TiledParams& prm, int slot, float* out, int i, const float* V,
+__device__ __forceinline__ void apply_ops(const TiledParams& prm, const OutMap& om, float* out, int i, const float* V,
                                           const float (*D)[3]) {
-    int col = 0;
     for (int o = 0; o < prm.n_ops; ++o) {
+        const int base = om.base[o];
+        if (base < 0) continue;
         const DOp& op = prm.ops[o];
-        if (op.slot != slot) continue;
         const float mult = op.mult_f;
-        float* x = out + col * kSub + i;
+        float* x = out + base + i * om.pstr[o];
+        const int cs = om.cstr[o];
         switch (op.kind) {
             case CGX_SCALAR_VALUE_G2P:
                 x[0] += mult * V[0];
-                col += 1;
                 break;
             case CGX_VECTOR_VALUE_G2P:
 #pragma unroll
-                for (int d = 0; d < 3; ++d) x[d * kSub] += mult * V[d < NDOF ? d : 0];
-                col += 3;
+                for (int d = 0; d < 3; ++d) x[d * cs] += mult * V[d < NDOF ? d : 0];
                 break;
             case CGX_SCALAR_GRADIENT_G2P:
 #pragma unroll
-                for (int d = 0; d < 3; ++d) x[d * kSub] += mult * D[d][0];
-                col += 3;
+                for (int d = 0; d < 3; ++d) x[d * cs] += mult * D[d][0];
                 break;
             case CGX_VECTOR_GRADIENT_G2P:
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
 #pragma unroll
-                    for (int b = 0; b < 3; ++b) x[(a * 3 + b) * kSub] += mult * D[a][b < NDOF ? b : 0];
-                col += 9;
+                    for (int b = 0; b < 3; ++b) x[(a * 3 + b) * cs] += mult * D[a][b < NDOF ? b : 0];
                 break;
             case CGX_VECTOR_GRADIENT_T_G2P:
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
 #pragma unroll
-                    for (int b = 0; b < 3; ++b) x[(b * 3 + a) * kSub] += mult * D[a][b < NDOF ? b : 0];
-                col += 9;
+                    for (int b = 0; b < 3; ++b) x[(b * 3 + a) * cs] += mult * D[a][b < NDOF ? b : 0];
                 break;
             case CGX_VECTOR_DIVERGENCE_G2P:
                 x[0] += (D[0][0] + D[1][1 < NDOF ? 1 : 0] + D[2][2 < NDOF ? 2 : 0]) * mult;
-                col += 1;
                 break;
         }
     }
@@ -206,6 +210,46 @@ __global__ void __launch_bounds__(kThreads, 2)
     int cur_inst = -1;
     const TiledGeom& geo = BATCHED ? sgeo : prm.geom;
     const int64_t nwork = *prm.work_count;
+    // Staging of the point fields of the operators reading array `slot`:
+    // operator o owns ncomp[o] * kSub + kOpSlack floats of `out` from
+    // region[o] (16-byte aligned; -1 for operators of other arrays). A dense
+    // FP32 field (vector length 1, its components adjacent) is staged in its
+    // own layout by one bulk copy per pass and written back by one bulk copy
+    // of its 16-byte aligned interior plus plain stores of the ragged ends;
+    // other fields are staged one component (kSub floats) at a time.
+    __shared__ int region[kMaxOps], ncomp[kMaxOps];
+    __shared__ float* dense_of[kMaxOps];  // per instance: the dense field, or null
+    __shared__ OutMap om;                 // per pass
+    // Bulk loads complete one phase of ld_bar per pass; a wait that runs out
+    // sets `aborted` for the CTA.
+    __shared__ uint64_t ld_bar;
+    __shared__ int aborted;
+    unsigned ld_phase = 0u;
+    if (threadIdx.x == 0) {
+        mbar_init(&ld_bar);
+        aborted = 0;
+        int base = 0;
+        for (int o = 0; o < prm.n_ops; ++o) {
+            const bool mine = prm.ops[o].slot == slot;
+            const int nc = mine ? dev_g2p_comps(prm.ops[o].kind) : 0;
+            region[o] = mine ? base : -1;
+            ncomp[o] = nc;
+            base += mine ? nc * kSub + kOpSlack : 0;
+        }
+    }
+    __syncthreads();
+    // Fill dense_of for the instance in `geo` (threads < n_ops; the caller
+    // synchronises before the next pass).
+    auto find_dense = [&]() {
+        if (threadIdx.x < prm.n_ops) {
+            const int o = threadIdx.x, nc = ncomp[o];
+            const DField f = geo.x[o];
+            const bool dense = region[o] >= 0 && f.log2vl == 0 && f.comp_stride == 1 && f.soa_stride == nc &&
+                               f.dtype == CGX_F32;
+            dense_of[o] = dense ? reinterpret_cast<float*>(f.data) : nullptr;
+        }
+    };
+    if (!BATCHED) find_dense();  // visible after the first item's barrier
     while (true) {
         if (threadIdx.x == 0) item_idx = atomicAdd(prm.work_counter, 1);
         __syncthreads();
@@ -218,6 +262,8 @@ __global__ void __launch_bounds__(kThreads, 2)
             int* dst = reinterpret_cast<int*>(&sgeo);
             for (int i = threadIdx.x; i < int(sizeof(TiledGeom) / 4); i += blockDim.x) dst[i] = src[i];
             cur_inst = it.instance;
+            __syncthreads();
+            find_dense();
             __syncthreads();
         }
         const DArray& arr = geo.arr[slot];
@@ -257,30 +303,60 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
         for (int64_t sb = it.begin; sb < it.end; sb += kSub) {
             const int len = int((it.end - sb < kSub) ? it.end - sb : kSub);
-            // 1. load. Current point-field values first, as asynchronous
-            // copies, one component at a time (the tiled path only takes FP32
-            // point fields); then the coordinates, all of a thread's particles
-            // loaded before any is used.
-            {
-                int col = 0;
-                for (int o = 0; o < prm.n_ops; ++o) {
-                    const DOp& op = prm.ops[o];
-                    if (op.slot != slot) continue;
-                    const DField& fx = geo.x[o];
-                    const int nc = dev_g2p_comps(op.kind);
-                    for (int c = 0; c < nc; ++c, ++col) {
-                        float* dst = out + col * kSub;
-                        if (fx.log2vl == 0) {
-                            const float* src = reinterpret_cast<const float*>(fx.data) + int64_t(c) * fx.comp_stride +
-                                               sb * fx.soa_stride;
-                            const int64_t stride = fx.soa_stride;
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, src + i * stride);
-                        } else {
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_field<float>(fx, sb + i, c);
+            // 1. load. Current point-field values first (bulk copies of dense
+            // fields, asynchronous copies of single components otherwise),
+            // then the coordinates, all of a thread's particles loaded
+            // before any is used.
+            if (threadIdx.x < prm.n_ops) {
+                const int o = threadIdx.x;
+                const float* d = dense_of[o];
+                if (region[o] < 0) {
+                    om.base[o] = -1;
+                } else if (d) {
+                    const int shift = int((reinterpret_cast<uintptr_t>(d + sb * ncomp[o]) >> 2) & 3);
+                    om.base[o] = region[o] + shift;
+                    om.pstr[o] = ncomp[o];
+                    om.cstr[o] = 1;
+                } else {
+                    om.base[o] = region[o];
+                    om.pstr[o] = 1;
+                    om.cstr[o] = kSub;
+                }
+            }
+            bool bulk = false;  // the same in every thread
+            for (int o = 0; o < prm.n_ops; ++o) {
+                if (region[o] < 0) continue;
+                const int nc = ncomp[o];
+                const float* d = dense_of[o];
+                if (d) {
+                    if (threadIdx.x == 0) {
+                        if (!bulk) {
+                            bulk_wait_read();     // the previous pass's write-back has read the region
+                            fence_proxy_async();  // after the barrier that ended the region's last accesses
                         }
+                        const float* first = d + sb * nc;
+                        const int shift = int((reinterpret_cast<uintptr_t>(first) >> 2) & 3);
+                        const unsigned bytes = unsigned((shift + len * nc + 3) >> 2) * 16u;
+                        mbar_expect_tx(&ld_bar, bytes);
+                        bulk_copy_g2s(out + region[o], first - shift, bytes, &ld_bar);
+                    }
+                    bulk = true;
+                    continue;
+                }
+                const DField& fx = geo.x[o];
+                for (int c = 0; c < nc; ++c) {
+                    float* dst = out + region[o] + c * kSub;
+                    if (fx.log2vl == 0) {
+                        const float* src =
+                            reinterpret_cast<const float*>(fx.data) + int64_t(c) * fx.comp_stride + sb * fx.soa_stride;
+                        const int64_t stride = fx.soa_stride;
+                        for (int i = threadIdx.x; i < len; i += blockDim.x) cp_async4(dst + i, src + i * stride);
+                    } else {
+                        for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = load_field<float>(fx, sb + i, c);
                     }
                 }
             }
+            if (bulk && threadIdx.x == 0) mbar_arrive(&ld_bar);
             {
                 constexpr int PER = kSub / kThreads;
                 double xs[PER][3];
@@ -314,7 +390,15 @@ __global__ void __launch_bounds__(kThreads, 2)
                 }
             }
             cp_async_wait_all();
+            if (bulk) {
+                if (!mbar_wait(&ld_bar, ld_phase, kMaxPolls)) {
+                    raise_error(prm.error_flag, CGX_ERR_TIMEOUT);
+                    aborted = 1;
+                }
+                ld_phase ^= 1u;
+            }
             __syncthreads();
+            if (aborted) break;  // the same in every thread after the barrier
             // 2. compute
             for (int i = threadIdx.x; i < len; i += blockDim.x) {
                 const float4 pu = prep[i];
@@ -336,34 +420,52 @@ __global__ void __launch_bounds__(kThreads, 2)
                     form_point<ORDER>(geo, sb + i, s, uu);
                     gather_sums<ORDER, TILE, NDOF, GRAD, false>(geo, arr, box, l, s, w, g, V, D);
                 }
-                apply_ops<NDOF>(prm, slot, out, i, V, D);
+                apply_ops<NDOF>(prm, om, out, i, V, D);
             }
+            fence_proxy_async();  // the staged values are read by bulk copies below
             __syncthreads();
             // 3. store
-            {
-                int col = 0;
-                for (int o = 0; o < prm.n_ops; ++o) {
-                    const DOp& op = prm.ops[o];
-                    if (op.slot != slot) continue;
-                    const DField& fx = geo.x[o];
-                    const int nc = dev_g2p_comps(op.kind);
-                    for (int c = 0; c < nc; ++c, ++col) {
-                        const float* srcv = out + col * kSub;
-                        if (fx.log2vl == 0) {
-                            float* dst = reinterpret_cast<float*>(fx.data) + int64_t(c) * fx.comp_stride +
-                                         sb * fx.soa_stride;
-                            const int64_t stride = fx.soa_stride;
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i * stride] = srcv[i];
-                        } else {
-                            float* data = reinterpret_cast<float*>(fx.data);
-                            for (int i = threadIdx.x; i < len; i += blockDim.x) data[field_offset(fx, sb + i, c)] = srcv[i];
-                        }
+            for (int o = 0; o < prm.n_ops; ++o) {
+                if (region[o] < 0) continue;
+                const int nc = ncomp[o];
+                float* d = dense_of[o];
+                if (d) {
+                    // elements [0, n) of the pass start at `first` and at
+                    // out[base]; [head, head + body) is 16-byte aligned at both
+                    float* first = d + sb * nc;
+                    const int base = om.base[o], n = len * nc;
+                    const int head = min(n, int((4 - ((reinterpret_cast<uintptr_t>(first) >> 2) & 3)) & 3));
+                    const int body = (n - head) & ~3;
+                    if (threadIdx.x == 0 && body > 0)
+                        bulk_copy_s2g(first + head, out + base + head, unsigned(body) * 4u);
+                    const int t = threadIdx.x;
+                    if (t < head) {
+                        first[t] = out[base + t];
+                    } else if (t >= 4 && t < 4 + (n - head - body)) {
+                        const int e = head + body + (t - 4);
+                        first[e] = out[base + e];
+                    }
+                    continue;
+                }
+                const DField& fx = geo.x[o];
+                for (int c = 0; c < nc; ++c) {
+                    const float* srcv = out + region[o] + c * kSub;
+                    if (fx.log2vl == 0) {
+                        float* dst = reinterpret_cast<float*>(fx.data) + int64_t(c) * fx.comp_stride + sb * fx.soa_stride;
+                        const int64_t stride = fx.soa_stride;
+                        for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i * stride] = srcv[i];
+                    } else {
+                        float* data = reinterpret_cast<float*>(fx.data);
+                        for (int i = threadIdx.x; i < len; i += blockDim.x) data[field_offset(fx, sb + i, c)] = srcv[i];
                     }
                 }
             }
+            if (threadIdx.x == 0) bulk_commit();
             __syncthreads();
         }
+        if (aborted) break;  // a bulk copy never completed: stop (the error flag is set)
     }
+    if (threadIdx.x == 0) bulk_wait_all();  // write-backs complete before the CTA exits
 }
 
 // launch == false: raise the shared-memory limit and report the resident
@@ -442,7 +544,9 @@ size_t g2p_tiled_smem(const TiledParams& prm, int slot) {
     bool grad;
     g2p_slot_need(prm, slot, ndof, grad);
     const size_t box = size_t((prm.box_nodes * (ndof == 3 ? 4 : 1) + 3) & ~3) * sizeof(float);
-    return box + size_t(kSub) * sizeof(float4) + size_t(cols) * kSub * sizeof(float);
+    int n_slot_ops = 0;
+    for (int o = 0; o < prm.n_ops; ++o) n_slot_ops += prm.ops[o].slot == slot ? 1 : 0;
+    return box + size_t(kSub) * sizeof(float4) + (size_t(cols) * kSub + size_t(n_slot_ops) * kOpSlack) * sizeof(float);
 }
 
 cudaError_t launch_g2p_tiled(const TiledParams& prm, int order, int slot, int sms, size_t smem, cudaStream_t st) {

@@ -231,6 +231,53 @@ def test_fused_ops_match_oracle(oracle, form_name, precision, tiled):
     assert abs(mass.view().double().sum().item() - m.sum()) <= 1e-6 * m.sum()
 
 
+@pytest.mark.parametrize("offset", [0, 1, 2, 3])
+def test_tiled_dense_fields_at_any_alignment(oracle, offset):
+    """Dense FP32 point fields starting at any 4-byte offset inside a larger
+    buffer: the tiled kernels stage them by bulk copies from the 16-byte
+    boundary at or below the first element and write G2P results back by a
+    bulk copy of the aligned interior plus plain stores of the ends. Values
+    of the buffer outside the field are never written."""
+    lg, mp = small_mesh()
+    rng = np.random.default_rng(50 + offset)
+    n = 5001
+    lo, hi = domain(mp)
+    pts = clumped_points(rng, n, lo, hi, 3, 0.6)
+    v = rng.normal(size=(n, 3))
+    x0 = rng.normal(size=(n, 9))
+    om = oracle_mesh(oracle, mp)
+    grid_ref = np.zeros(mp.extents() + (3,))
+    assert oracle.p2g(om, pts, 2, [(1, 1.5, v, grid_ref)]) == 0
+    tp, (tv, tx), til, perm = sorted_inputs(mp, 2, pts, [v, x0], True)
+
+    def embed(t):
+        flat = t.float().reshape(-1)
+        buf = torch.full((flat.numel() + 8,), 7.0, device="cuda")
+        buf[offset:offset + flat.numel()] = flat
+        return buf, buf[offset:offset + flat.numel()].view(t.shape)
+
+    _, tv32 = embed(tv)
+    xbuf, tx32 = embed(tx.reshape(n, 3, 3))
+    arr = G.createArray("a", layout(lg, 3), torch.float32)
+    G.p2g(G.createVectorValueP2G(tv32, 1.5), tp, n, G.Spline(2), None, arr, precision=G.FP32_COMPENSATED, tiling=til)
+    assert G.last_dispatch() == "tiled"
+    assert max_rel(arr.view().double().cpu().numpy(), grid_ref) <= TOL_P2G_FP32
+
+    grid = rng.normal(size=mp.extents() + (3,))
+    ref = x0.copy()
+    assert oracle.g2p(om, pts, 2, [(3, -0.5, ref, grid.copy())]) == 0
+    garr = G.createArray("g", layout(lg, 3), torch.float32)
+    garr.view().copy_(torch.tensor(grid, device="cuda").float())
+    G.g2p(garr, None, tp, n, G.Spline(2), G.createVectorGradientG2P(tx32, -0.5), precision=G.FP32_COMPENSATED,
+          tiling=til)
+    assert G.last_dispatch() == "tiled"
+    got = tx32.double().cpu().numpy().reshape(n, 9)
+    ref, x0p = ref[perm], x0[perm]
+    assert max_rel(got - x0p, ref - x0p) <= TOL_G2P_FP32
+    guard = torch.cat([xbuf[:offset], xbuf[offset + 9 * n:]])
+    assert bool(torch.all(guard == 7.0))
+
+
 def test_aosoa_and_layout_left_fields(oracle):
     """Slice (AoSoA, VL=32) and LayoutLeft particle fields give the same result."""
     lg, mp = small_mesh()
