@@ -167,6 +167,17 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
+// L2 prefetch of particles [b, e) of a field stored densely per particle
+// (vector length 1, components adjacent) by one bulk prefetch of the 16-byte
+// blocks holding them, issued by thread 0; other layouts are left alone.
+__device__ __forceinline__ void prefetch_field_range(const DField& f, int64_t b, int64_t e) {
+    if (threadIdx.x != 0 || f.log2vl != 0 || f.comp_stride != 1 || e <= b) return;
+    const int64_t elt = f.dtype == CGX_F64 ? 8 : 4;
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(f.data + b * f.soa_stride * elt) & ~uintptr_t(15);
+    const uintptr_t hi = (reinterpret_cast<uintptr_t>(f.data + e * f.soa_stride * elt) + 15) & ~uintptr_t(15);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"(unsigned(hi - lo)) : "memory");
+}
+
 // Ask the L1 to fetch the line holding element (p, c) of a field.
 __device__ __forceinline__ void prefetch_field(const DField& f, int64_t p, int c) {
     const int64_t o = field_offset(f, p, c) * (f.dtype == CGX_F64 ? 8 : 4);

@@ -138,17 +138,6 @@ __device__ __forceinline__ float load_src(const TiledGeom& geo, const Source& sr
                               : __ldg(reinterpret_cast<const float*>(f.data) + o);
 }
 
-// L2 prefetch of particles [b, e) of a field stored densely per particle
-// (vector length 1, components adjacent); other layouts are left alone.
-__device__ __forceinline__ void prefetch_field_range(const DField& f, int64_t b, int64_t e) {
-    if (f.log2vl != 0 || f.comp_stride != 1) return;
-    const int64_t elt = f.dtype == CGX_F64 ? 8 : 4;
-    const char* base = f.data + b * f.soa_stride * elt;
-    const int64_t bytes = (e - b) * f.soa_stride * elt;
-    for (int64_t o = int64_t(threadIdx.x) * 128; o < bytes; o += int64_t(blockDim.x) * 128)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + o));
-}
-
 __device__ __forceinline__ void prefetch_item(const TiledGeom* g, int n_ops, int64_t b, int64_t e) {
     prefetch_field_range(g->points, b, e);
     for (int o = 0; o < n_ops; ++o) prefetch_field_range(g->x[o], b, e);
@@ -579,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             if (threadIdx.x == 0) n_big = 0;
             const int len = int(it.end - cb < kChunk ? it.end - cb : kChunk);
             const bool bulk = stage(cb, len);
-            {
+            if (threadIdx.x == 0) {
                 // Pull the next chunk's coordinates and operator inputs (of
                 // this item, or the first chunk of the next one) into L2 while
                 // this chunk is processed: its prep then waits on L2, not HBM.
