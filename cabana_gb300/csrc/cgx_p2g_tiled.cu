@@ -18,7 +18,7 @@
 //    spline) so a lane holds its group's whole stencil (27 nodes x channels)
 //    in registers. The CTA's 16 warps pull units of work -- (piece, group)
 //    and then (window, group) -- from shared counters.
-//  * Runs of two or more particles are cut into pieces of <= 256 particles
+//  * Runs of two or more particles are cut into pieces of <= 512 particles
 //    (a dense cell keeps every warp busy). A piece is walked 32 particles at
 //    a time, one particle per lane, each lane adding its particle into its registers; at the end of
 //    the piece the warp reduces the registers across lanes with a
@@ -49,7 +49,7 @@ constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows pe
 constexpr int kSmallRun = 2;        // shorter runs (single particles) add each particle directly
 // Long runs are cut into pieces of at most kPiece particles so that all the
 // warps of a channel group share a dense cell, each piece reduced on its own.
-constexpr int kPiece = 256;
+constexpr int kPiece = 512;
 constexpr int kMaxPieces = kChunk / kSmallRun + kChunk / kPiece + 1;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
@@ -198,29 +198,34 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGe
 }
 
 // Register accumulation of this lane's particle (zero coefficients for lanes
-// outside the current run).
+// outside the current run). The coefficients are folded into the x-weights
+// first, so each (i, j) pair costs one product per channel (value) or three
+// (gradient) before the K fused multiply-adds per node.
 template <int ORDER, int CH, bool GRAD>
 __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
                                            const float (*coef)[3], bool member) {
     constexpr int K = ORDER + 1;
-    float cm[CH][3];
+    if (GRAD) {
+        // node (i, j, k) += P_ij w_k + Q_ij g_k with
+        // P_ij = c0 g_i w_j + c1 w_i g_j and Q_ij = c2 w_i w_j
+        float a0[CH][K], a1[CH][K], a2[CH][K];
 #pragma unroll
-    for (int c = 0; c < CH; ++c)
+        for (int c = 0; c < CH; ++c)
 #pragma unroll
-        for (int n = 0; n < 3; ++n) cm[c][n] = member ? coef[c][n] : 0.0f;
+            for (int i = 0; i < K; ++i) {
+                a0[c][i] = member ? coef[c][0] * g[0][i] : 0.0f;
+                a1[c][i] = member ? coef[c][1] * w[0][i] : 0.0f;
+                a2[c][i] = member ? coef[c][2] * w[0][i] : 0.0f;
+            }
 #pragma unroll
-    for (int i = 0; i < K; ++i)
+        for (int i = 0; i < K; ++i)
 #pragma unroll
-        for (int j = 0; j < K; ++j) {
-            if (GRAD) {
-                const float wij = w[0][i] * w[1][j];
-                const float gi0 = g[0][i] * w[1][j];
-                const float gi1 = w[0][i] * g[1][j];
+            for (int j = 0; j < K; ++j) {
                 float P[CH], Q[CH];
 #pragma unroll
                 for (int c = 0; c < CH; ++c) {
-                    P[c] = cm[c][0] * gi0 + cm[c][1] * gi1;
-                    Q[c] = cm[c][2] * wij;
+                    P[c] = fmaf(a0[c][i], w[1][j], a1[c][i] * g[1][j]);
+                    Q[c] = a2[c][i] * w[1][j];
                 }
 #pragma unroll
                 for (int k = 0; k < K; ++k)
@@ -229,11 +234,21 @@ __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 
                         float& a = acc[((i * K + j) * K + k) * CH + c];
                         a = fmaf(P[c], w[2][k], fmaf(Q[c], g[2][k], a));
                     }
-            } else {
-                const float wij = w[0][i] * w[1][j];
+            }
+    } else {
+        // node (i, j, k) += (c0 w_i) w_j w_k
+        float a0[CH][K];
+#pragma unroll
+        for (int c = 0; c < CH; ++c)
+#pragma unroll
+            for (int i = 0; i < K; ++i) a0[c][i] = member ? coef[c][0] * w[0][i] : 0.0f;
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
                 float A[CH];
 #pragma unroll
-                for (int c = 0; c < CH; ++c) A[c] = cm[c][0] * wij;
+                for (int c = 0; c < CH; ++c) A[c] = a0[c][i] * w[1][j];
 #pragma unroll
                 for (int k = 0; k < K; ++k)
 #pragma unroll
@@ -242,7 +257,7 @@ __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 
                         a = fmaf(A[c], w[2][k], a);
                     }
             }
-        }
+    }
 }
 
 // Reduce the warp's register sums and add them to the box.
