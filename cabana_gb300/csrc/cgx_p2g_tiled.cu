@@ -18,7 +18,7 @@
 //    spline) so a lane holds its group's whole stencil (27 nodes x channels)
 //    in registers. The CTA's 16 warps pull units of work -- (piece, group)
 //    and then (window, group) -- from shared counters.
-//  * Runs of two or more particles are cut into pieces of <= 512 particles
+//  * Runs of two or more particles are cut into pieces of <= 1024 particles
 //    (a dense cell keeps every warp busy). A piece is walked 32 particles at
 //    a time, one particle per lane, each lane adding its particle into its registers; at the end of
 //    the piece the warp reduces the registers across lanes with a
@@ -49,7 +49,7 @@ constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows pe
 constexpr int kSmallRun = 2;        // shorter runs (single particles) add each particle directly
 // Long runs are cut into pieces of at most kPiece particles so that all the
 // warps of a channel group share a dense cell, each piece reduced on its own.
-constexpr int kPiece = 512;
+constexpr int kPiece = 1024;
 constexpr int kMaxPieces = kChunk / kSmallRun + kChunk / kPiece + 1;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
