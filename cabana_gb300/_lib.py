@@ -54,6 +54,8 @@ class CgxMesh(ctypes.Structure):
         ("halo_width", ctypes.c_int32),
         ("periodic", ctypes.c_int32 * 3),
         ("entity", ctypes.c_int32),
+        ("num_space_dim", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 
@@ -185,15 +187,17 @@ def check(status):
 
 
 def make_mesh(params):
-    """CgxMesh from a cabana_gb300.mesh.MeshParams."""
+    """CgxMesh from a cabana_gb300.mesh.MeshParams (3D or 2D)."""
     m = CgxMesh()
+    nd = getattr(params, "num_space_dim", 3)
     for d in range(3):
-        m.ghost_low[d] = params.ghost_low[d]
-        m.cell_size[d] = params.cell_size[d]
-        m.owned_cells[d] = params.owned_cells[d]
-        m.periodic[d] = params.periodic[d]
+        m.ghost_low[d] = params.ghost_low[d] if d < nd else 0.0
+        m.cell_size[d] = params.cell_size[d] if d < nd else 1.0
+        m.owned_cells[d] = params.owned_cells[d] if d < nd else 1
+        m.periodic[d] = params.periodic[d] if d < nd else 0
     m.halo_width = params.halo_width
     m.entity = params.entity
+    m.num_space_dim = nd
     return m
 
 

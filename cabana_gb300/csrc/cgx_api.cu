@@ -56,15 +56,21 @@ cgx_status ensure_ws(cgx_context* h, size_t bytes) {
 
 bool valid_dtype(int t) { return t == CGX_F32 || t == CGX_F64; }
 
+// Space dimensions of a mesh (num_space_dim 0 reads as 3).
+int mesh_dims(const cgx_mesh& m) { return m.num_space_dim == 2 ? 2 : 3; }
+
 cgx_status check_mesh(const cgx_mesh* m) {
     if (!m) return fail(CGX_ERR_INVALID_ARG, "mesh is NULL");
-    for (int d = 0; d < 3; ++d) {
+    if (m->num_space_dim != 0 && m->num_space_dim != 2 && m->num_space_dim != 3)
+        return fail(CGX_ERR_INVALID_ARG, "num_space_dim must be 2 or 3");
+    const int nd = mesh_dims(*m);
+    for (int d = 0; d < nd; ++d) {
         if (!(m->cell_size[d] > 0.0)) return fail(CGX_ERR_INVALID_ARG, "cell_size must be positive");
         if (m->owned_cells[d] < 1) return fail(CGX_ERR_INVALID_ARG, "owned_cells must be >= 1");
     }
     if (m->halo_width < 0) return fail(CGX_ERR_INVALID_ARG, "halo_width must be >= 0");
     if (m->entity != CGX_NODE && m->entity != CGX_CELL) return fail(CGX_ERR_INVALID_ARG, "entity must be CGX_NODE or CGX_CELL");
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < nd; ++d) {
         if (m->periodic[d] && m->halo_width >= m->owned_cells[d])
             return fail(CGX_ERR_INVALID_ARG, "periodic halo wider than the owned cells");
     }
@@ -92,9 +98,18 @@ DField to_dfield(const cgx_field& f) {
 
 // LocalMesh::coordinates(Entity, index) (grid/src/Cabana_Grid_LocalMesh.hpp:
 // 180-200) and the dx / rdx of evaluateSpline (Splines.hpp:1293-1311).
+// A 2D mesh has one entity layer in the third dimension (ext 1), so its
+// (i, j, dof) arrays index as (i, j, 0, dof).
 DMesh to_dmesh(const cgx_mesh& m) {
     DMesh d;
     for (int a = 0; a < 3; ++a) {
+        if (a >= mesh_dims(m)) {
+            d.low[a] = 0.0;
+            d.rdx[a] = 1.0;
+            d.rdx_f[a] = 1.0f;
+            d.ext[a] = 1;
+            continue;
+        }
         double lo, hi;
         if (m.entity == CGX_CELL) {
             lo = m.ghost_low[a] + (double(0) + double(0.5)) * m.cell_size[a];
@@ -112,62 +127,71 @@ DMesh to_dmesh(const cgx_mesh& m) {
     return d;
 }
 
-int p2g_comps(int kind) {
+// Point components and array dofs of each operator kind in nd space
+// dimensions: scalars 1, vectors nd, tensors nd * nd.
+int p2g_comps(int kind, int nd = 3) {
     switch (kind) {
         case CGX_SCALAR_VALUE_P2G: case CGX_SCALAR_GRADIENT_P2G: return 1;
-        case CGX_VECTOR_VALUE_P2G: case CGX_VECTOR_DIVERGENCE_P2G: return 3;
-        case CGX_TENSOR_DIVERGENCE_P2G: case CGX_TENSOR_DIVERGENCE_T_P2G: return 9;
+        case CGX_VECTOR_VALUE_P2G: case CGX_VECTOR_DIVERGENCE_P2G: return nd;
+        case CGX_TENSOR_DIVERGENCE_P2G: case CGX_TENSOR_DIVERGENCE_T_P2G: return nd * nd;
     }
     return -1;
 }
-int p2g_dofs(int kind) {
+int p2g_dofs(int kind, int nd = 3) {
     switch (kind) {
         case CGX_SCALAR_VALUE_P2G: case CGX_VECTOR_DIVERGENCE_P2G: return 1;
         case CGX_VECTOR_VALUE_P2G: case CGX_SCALAR_GRADIENT_P2G: case CGX_TENSOR_DIVERGENCE_P2G:
-        case CGX_TENSOR_DIVERGENCE_T_P2G: return 3;
+        case CGX_TENSOR_DIVERGENCE_T_P2G: return nd;
     }
     return -1;
 }
-int g2p_comps(int kind) {
+int g2p_comps(int kind, int nd = 3) {
     switch (kind) {
         case CGX_SCALAR_VALUE_G2P: case CGX_VECTOR_DIVERGENCE_G2P: return 1;
-        case CGX_VECTOR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 3;
-        case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_GRADIENT_T_G2P: return 9;
+        case CGX_VECTOR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return nd;
+        case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_GRADIENT_T_G2P: return nd * nd;
     }
     return -1;
 }
-int g2p_dofs(int kind) {
+int g2p_dofs(int kind, int nd = 3) {
     switch (kind) {
         case CGX_SCALAR_VALUE_G2P: case CGX_SCALAR_GRADIENT_G2P: return 1;
         case CGX_VECTOR_VALUE_G2P: case CGX_VECTOR_GRADIENT_G2P: case CGX_VECTOR_DIVERGENCE_G2P:
-        case CGX_VECTOR_GRADIENT_T_G2P: return 3;
+        case CGX_VECTOR_GRADIENT_T_G2P: return nd;
     }
     return -1;
 }
 
-bool any_periodic(const cgx_mesh& m) { return m.periodic[0] || m.periodic[1] || m.periodic[2]; }
+bool any_periodic(const cgx_mesh& m) {
+    bool any = false;
+    for (int d = 0; d < mesh_dims(m); ++d) any |= m.periodic[d] != 0;
+    return any;
+}
 
 HaloParams to_halo(const cgx_mesh& m, const cgx_array& a) {
     HaloParams h;
     h.data = reinterpret_cast<char*>(a.data);
     h.dtype = a.dtype;
     h.dofs = a.dofs;
+    h.dims = mesh_dims(m);
+    h.reserved = 0;
     for (int d = 0; d < 3; ++d) {
-        h.ext[d] = m.owned_cells[d] + 2 * m.halo_width + (m.entity == CGX_NODE ? 1 : 0);
-        h.owned_cells[d] = m.owned_cells[d];
-        h.periodic[d] = m.periodic[d] ? 1 : 0;
+        const bool in = d < h.dims;
+        h.ext[d] = in ? m.owned_cells[d] + 2 * m.halo_width + (m.entity == CGX_NODE ? 1 : 0) : 1;
+        h.owned_cells[d] = in ? m.owned_cells[d] : 1;
+        h.periodic[d] = in && m.periodic[d] ? 1 : 0;
     }
     h.halo_width = m.halo_width;
     h.node_extra = m.entity == CGX_NODE ? 1 : 0;
     return h;
 }
 
-cgx_status check_ops(const cgx_op* ops, int n_ops, bool p2g, bool have_points) {
+cgx_status check_ops(const cgx_op* ops, int n_ops, bool p2g, bool have_points, int nd = 3) {
     if (!ops || n_ops < 1 || n_ops > kMaxOps) return fail(CGX_ERR_INVALID_ARG, "n_ops must be in [1, 8]");
     for (int o = 0; o < n_ops; ++o) {
         const cgx_op& op = ops[o];
-        const int comps = p2g ? p2g_comps(op.kind) : g2p_comps(op.kind);
-        const int dofs = p2g ? p2g_dofs(op.kind) : g2p_dofs(op.kind);
+        const int comps = p2g ? p2g_comps(op.kind, nd) : g2p_comps(op.kind, nd);
+        const int dofs = p2g ? p2g_dofs(op.kind, nd) : g2p_dofs(op.kind, nd);
         if (comps < 0) return fail(CGX_ERR_INVALID_ARG, "unknown operator kind");
         if (have_points) {
             cgx_status s = check_field(&op.x, "op.x");
@@ -434,7 +458,8 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
     if (spline_order < 0 || spline_order > 6) return fail(CGX_ERR_NOT_SUPPORTED, "spline order must be in [0, 6]");
     if (precision != CGX_PLAIN_FP64 && precision != CGX_FP32_COMPENSATED)
         return fail(CGX_ERR_INVALID_ARG, "unknown precision");
-    s = check_ops(ops, n_ops, p2g, num_point > 0);
+    const int nd = mesh_dims(*mesh);
+    s = check_ops(ops, n_ops, p2g, num_point > 0, nd);
     if (s) return s;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (flags & CGX_FLAG_CHECK_BOUNDS) CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
@@ -447,7 +472,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
 
     // The tiled kernels are built for cubic tiles of kTiledTile base nodes;
     // other tilings still order the particles but run the point kernels.
-    bool tiled = num_point > 0 && tiling && precision == CGX_FP32_COMPENSATED && tiling->tile_offsets &&
+    bool tiled = nd == 3 && num_point > 0 && tiling && precision == CGX_FP32_COMPENSATED && tiling->tile_offsets &&
                  tiling->spline_order == spline_order && spline_order >= 1 && spline_order <= 3 &&
                  tiling->tile[0] == kTiledTile && tiling->tile[1] == kTiledTile && tiling->tile[2] == kTiledTile;
     if (tiled) {
@@ -487,6 +512,7 @@ cgx_status interpolate(cgx_handle h, const cgx_mesh* mesh, const cgx_field* poin
         prm.points = to_dfield(*points);
         prm.num_point = num_point;
         prm.n_ops = n_ops;
+        prm.dims = nd;
         prm.error_flag = h->flags;
         for (int o = 0; o < n_ops; ++o) {
             prm.ops[o].kind = ops[o].kind;
@@ -572,6 +598,7 @@ cgx_status adjoint(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, 
     if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
     cgx_status s = check_mesh(mesh);
     if (s) return s;
+    if (mesh_dims(*mesh) != 3) return fail(CGX_ERR_NOT_SUPPORTED, "adjoints are built for 3D meshes");
     if (num_point < 0) return fail(CGX_ERR_INVALID_ARG, "num_point must be >= 0");
     if (num_point > 0) {
         s = check_field(points, "points");
@@ -905,6 +932,7 @@ cgx_status cgx_permute(cgx_handle h, const uint64_t* permutes, int64_t begin, in
 cgx_status cgx_tiling_init(const cgx_mesh* mesh, int spline_order, const int32_t tile[3], cgx_tiling* out) {
     cgx_status s = check_mesh(mesh);
     if (s) return s;
+    if (mesh_dims(*mesh) != 3) return fail(CGX_ERR_NOT_SUPPORTED, "tilings are built for 3D meshes");
     if (!tile || !out) return fail(CGX_ERR_INVALID_ARG, "NULL argument");
     if (spline_order < 0 || spline_order > 6) return fail(CGX_ERR_NOT_SUPPORTED, "spline order must be in [0, 6]");
     const DMesh dm = to_dmesh(*mesh);
@@ -935,6 +963,7 @@ cgx_status cgx_sort_tiles(cgx_handle h, const cgx_mesh* mesh, const cgx_field* p
     if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
     cgx_status s = check_mesh(mesh);
     if (s) return s;
+    if (mesh_dims(*mesh) != 3) return fail(CGX_ERR_NOT_SUPPORTED, "tilings are built for 3D meshes");
     s = check_field(points, "points");
     if (s) return s;
     if (points->dtype != CGX_F64) return fail(CGX_ERR_INVALID_ARG, "point coordinates must be double");
@@ -1072,6 +1101,7 @@ cgx_status cgx_batch_plan_create(cgx_handle h, const cgx_instance* inst, int n_i
     for (int i = 0; i < n_inst; ++i) {
         const cgx_instance& I = inst[i];
         cgx_status s = check_mesh(&I.mesh);
+        if (!s && mesh_dims(I.mesh) != 3) s = fail(CGX_ERR_NOT_SUPPORTED, "batched launches are built for 3D meshes");
         if (s) return s;
         if (I.num_point < 0) return fail(CGX_ERR_INVALID_ARG, "num_point must be >= 0");
         s = check_field(&I.points, "points");

@@ -10,7 +10,7 @@ struct PointParams {
     DField points;
     int64_t num_point;
     int32_t n_ops;
-    int32_t reserved;
+    int32_t dims;  // 3, or 2 for a 2D mesh (mesh.ext[2] == 1; points hold 2 coordinates)
     int* error_flag;
     DOp ops[kMaxOps];
 };
@@ -24,6 +24,8 @@ struct HaloParams {
     int32_t periodic[3];
     int32_t halo_width;
     int32_t node_extra;  // 1 for nodes, 0 for cells
+    int32_t dims;        // 3, or 2 (the single k layer of a 2D array is owned)
+    int32_t reserved;
 };
 
 // One distinct grid array touched by a tiled launch.

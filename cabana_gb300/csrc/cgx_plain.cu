@@ -262,6 +262,154 @@ __global__ void __launch_bounds__(256) g2p_points_kernel(const __grid_constant__
 }
 
 // ---------------------------------------------------------------------------
+// 2D meshes: the same two kernels over (i, j) stencils, an Array (i, j, dof)
+// indexed as (i, j, 0, dof) with mesh.ext[2] == 1, vectors of 2 components
+// and 2 x 2 tensors (the 2D specialisations of
+// grid/src/Cabana_Grid_Interpolation.hpp:81-396 and :466-788).
+// ---------------------------------------------------------------------------
+template <int ORDER, class T>
+__device__ __forceinline__ bool weights_2d(const PointParams& prm, int64_t p, int* s, T (*w)[ORDER + 1],
+                                           T (*g)[ORDER + 1]) {
+    using S = SplineKernel<ORDER, T>;
+    constexpr int nk = S::nk;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        const double xp = load_field<double>(prm.points, p, d);
+        const double x0 = logical_coord<ORDER>(xp, prm.mesh.low[d], prm.mesh.rdx[d]);
+        T u;
+        base_and_offset<ORDER, T>(x0, s[d], u);
+        ok &= (x0 >= 0.0) && (s[d] >= 0) && (s[d] + nk <= prm.mesh.ext[d]);
+        if constexpr (sizeof(T) == 8)
+            S::weights(u, prm.mesh.rdx[d], w[d], g[d]);
+        else
+            S::weights(u, prm.mesh.rdx_f[d], w[d], g[d]);
+    }
+    return ok;
+}
+
+template <int ORDER, class T>
+__global__ void __launch_bounds__(256) p2g_points_2d_kernel(const __grid_constant__ PointParams prm) {
+    constexpr int nk = ORDER + 1;
+    constexpr int U = ORDER <= 3 ? nk : 1;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < prm.num_point; p += stride) {
+        int s[2];
+        T w[2][nk], g[2][nk];
+        if (!weights_2d<ORDER, T>(prm, p, s, w, g)) {
+            raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+            continue;
+        }
+        for (int o = 0; o < prm.n_ops; ++o) {
+            const DOp& op = prm.ops[o];
+            const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
+            const int kind = op.kind;
+            // point data, premultiplied as the functors do (scalar: x * m,
+            // vector / tensor: m * x)
+            T pd[4] = {T(0), T(0), T(0), T(0)};
+            if (kind == CGX_SCALAR_VALUE_P2G || kind == CGX_SCALAR_GRADIENT_P2G) {
+                pd[0] = load_field<T>(op.x, p, 0) * mult;
+            } else if (kind == CGX_VECTOR_VALUE_P2G || kind == CGX_VECTOR_DIVERGENCE_P2G) {
+                pd[0] = mult * load_field<T>(op.x, p, 0);
+                pd[1] = mult * load_field<T>(op.x, p, 1);
+            } else {
+                // pd[2 m + n]: the entry paired with dW/dx_n for grid dof m
+                const bool tr = kind == CGX_TENSOR_DIVERGENCE_T_P2G;
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) pd[a * 2 + b] = mult * load_field<T>(op.x, p, tr ? b * 2 + a : a * 2 + b);
+            }
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j) {
+                    const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, 0);
+                    const T wij = w[0][i] * w[1][j];
+                    const T rg[2] = {g[0][i] * w[1][j], w[0][i] * g[1][j]};
+                    switch (kind) {
+                        case CGX_SCALAR_VALUE_P2G: atomic_add_array(op.a, n, 0, pd[0] * wij); break;
+                        case CGX_VECTOR_VALUE_P2G:
+                            atomic_add_array(op.a, n, 0, pd[0] * wij);
+                            atomic_add_array(op.a, n, 1, pd[1] * wij);
+                            break;
+                        case CGX_SCALAR_GRADIENT_P2G:
+                            atomic_add_array(op.a, n, 0, pd[0] * rg[0]);
+                            atomic_add_array(op.a, n, 1, pd[0] * rg[1]);
+                            break;
+                        case CGX_VECTOR_DIVERGENCE_P2G: atomic_add_array(op.a, n, 0, pd[0] * rg[0] + pd[1] * rg[1]); break;
+                        default:
+                            atomic_add_array(op.a, n, 0, rg[0] * pd[0] + rg[1] * pd[1]);
+                            atomic_add_array(op.a, n, 1, rg[0] * pd[2] + rg[1] * pd[3]);
+                            break;
+                    }
+                }
+        }
+    }
+}
+
+template <int ORDER, class T>
+__global__ void __launch_bounds__(256) g2p_points_2d_kernel(const __grid_constant__ PointParams prm) {
+    constexpr int nk = ORDER + 1;
+    constexpr int U = ORDER <= 3 ? nk : 1;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < prm.num_point; p += stride) {
+        int s[2];
+        T w[2][nk], g[2][nk];
+        if (!weights_2d<ORDER, T>(prm, p, s, w, g)) {
+            raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+            continue;
+        }
+        for (int o = 0; o < prm.n_ops; ++o) {
+            const DOp& op = prm.ops[o];
+            const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
+            const int kind = op.kind;
+            const bool vec = !(kind == CGX_SCALAR_VALUE_G2P || kind == CGX_SCALAR_GRADIENT_G2P);
+            // value sums V_c = sum W f_c and gradient sums D[m][c] = sum dW/dx_m f_c
+            T V[2] = {T(0), T(0)}, D[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j) {
+                    const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, 0);
+                    const T wij = w[0][i] * w[1][j];
+                    const T rg[2] = {g[0][i] * w[1][j], w[0][i] * g[1][j]};
+                    const T f0 = load_array<T>(op.a, n, 0);
+                    const T f1 = vec ? load_array<T>(op.a, n, 1) : T(0);
+                    V[0] += f0 * wij;
+                    V[1] += f1 * wij;
+#pragma unroll
+                    for (int m = 0; m < 2; ++m) {
+                        D[m][0] += rg[m] * f0;
+                        D[m][1] += rg[m] * f1;
+                    }
+                }
+            switch (kind) {
+                case CGX_SCALAR_VALUE_G2P: add_field<T>(op.x, p, 0, mult * V[0]); break;
+                case CGX_VECTOR_VALUE_G2P:
+                    add_field<T>(op.x, p, 0, mult * V[0]);
+                    add_field<T>(op.x, p, 1, mult * V[1]);
+                    break;
+                case CGX_SCALAR_GRADIENT_G2P:
+                    add_field<T>(op.x, p, 0, mult * D[0][0]);
+                    add_field<T>(op.x, p, 1, mult * D[1][0]);
+                    break;
+                case CGX_VECTOR_GRADIENT_G2P:
+                case CGX_VECTOR_GRADIENT_T_G2P: {
+                    const bool tr = kind == CGX_VECTOR_GRADIENT_T_G2P;
+#pragma unroll
+                    for (int a = 0; a < 2; ++a)
+#pragma unroll
+                        for (int b = 0; b < 2; ++b) add_field<T>(op.x, p, tr ? b * 2 + a : a * 2 + b, mult * D[a][b]);
+                    break;
+                }
+                case CGX_VECTOR_DIVERGENCE_G2P: add_field<T>(op.x, p, 0, (D[0][0] + D[1][1]) * mult); break;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Halo on one rank. A ghost entity has an owned partner when every
 // dimension in which it lies outside the owned range is periodic
 // (LocalGrid_impl.hpp:430-510 shared spaces; HaloBase.hpp unpack).
@@ -272,6 +420,10 @@ __device__ __forceinline__ bool halo_partner(const HaloParams& h, int i, int j, 
     bool ghost = false;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+        if (d >= h.dims) {
+            o[d] = idx[d];
+            continue;
+        }
         const int hw = h.halo_width, nc = h.owned_cells[d];
         const int own_hi = h.periodic[d] ? hw + nc : hw + nc + h.node_extra;
         if (idx[d] >= hw && idx[d] < own_hi) {
@@ -337,6 +489,20 @@ template <int ORDER>
 static cudaError_t launch_points_order(const PointParams& prm, bool p2g, bool fp64, int sms, cudaStream_t st) {
     const int threads = 256;
     const int blocks = grid_blocks(prm.num_point, threads, sms);
+    if (prm.dims == 2) {
+        if (p2g) {
+            if (fp64)
+                p2g_points_2d_kernel<ORDER, double><<<blocks, threads, 0, st>>>(prm);
+            else
+                p2g_points_2d_kernel<ORDER, float><<<blocks, threads, 0, st>>>(prm);
+        } else {
+            if (fp64)
+                g2p_points_2d_kernel<ORDER, double><<<blocks, threads, 0, st>>>(prm);
+            else
+                g2p_points_2d_kernel<ORDER, float><<<blocks, threads, 0, st>>>(prm);
+        }
+        return cudaGetLastError();
+    }
     if (p2g) {
         if (fp64)
             p2g_points_kernel<ORDER, double><<<blocks, threads, 0, st>>>(prm);

@@ -45,7 +45,8 @@ class Spline:
 
 
 class NodeHaloPattern:
-    """NodeHaloPattern<3>: the 26 face/edge/corner neighbours."""
+    """NodeHaloPattern<3> (26 neighbours) or NodeHaloPattern<2> (8): on one
+    rank both reduce to the periodic fold / fill of the mesh's dimensions."""
 
 
 def _dtype_code(t):
@@ -121,8 +122,9 @@ def createArrayLayout(local_grid, dofs_per_entity, entity=Node):
 
 
 class Array:
-    """Cabana::Grid::Array: a (i, j, k, dof) tensor over the ghosted index
-    space (grid/src/Cabana_Grid_Array.hpp:44-300)."""
+    """Cabana::Grid::Array: a (i, j, k, dof) tensor -- (i, j, dof) on a 2D
+    mesh -- over the ghosted index space (grid/src/Cabana_Grid_Array.hpp:
+    44-300)."""
 
     def __init__(self, label, layout: ArrayLayout, dtype=torch.float64, device="cuda", data=None):
         self.label = label
@@ -133,7 +135,7 @@ class Array:
         else:
             # wrap existing contiguous storage (e.g. a slice of a pooled buffer)
             if tuple(data.shape) != ext + (layout.dofs,) or not data.is_contiguous():
-                raise ValueError("data must be a contiguous (i, j, k, dof) tensor of the layout's extents")
+                raise ValueError("data must be a contiguous (i, j, [k,] dof) tensor of the layout's extents")
             self._view = data
 
     def layout(self):
@@ -184,8 +186,8 @@ class ArrayOp:
             L.check(L.lib().cgx_array_assign(ctypes.byref(array.mesh()), ctypes.byref(array.descriptor()),
                                              float(value), _stream(stream)))
         else:
-            (i0, i1), (j0, j1), (k0, k1) = array.layout().local_grid.ownedSpace(array.layout().entity)
-            array.view()[i0:i1, j0:j1, k0:k1] = value
+            own = array.layout().local_grid.ownedSpace(array.layout().entity)
+            array.view()[tuple(slice(a, b) for a, b in own)] = value
 
 
 # ---- functors ----------------------------------------------------------

@@ -12,6 +12,10 @@ Reference behaviour followed here:
   * LocalMesh<UniformMesh>: grid/src/Cabana_Grid_LocalMesh.hpp:61-120
     (ghost low corner = own low corner - halo * cell_size)
 
+A mesh is 3D or 2D (UniformMesh<double, 3> / <double, 2>): the number of
+entries of the corners passed to createUniformGlobalMesh sets it, and every
+per-dimension tuple below has that many entries.
+
 Pure Python; no GPU and no compiled code is needed to use it.
 """
 import math
@@ -37,9 +41,13 @@ class Cell:
 
 @dataclass
 class GlobalMesh:
-    low_corner: Tuple[float, float, float]
-    high_corner: Tuple[float, float, float]
-    cell_size: Tuple[float, float, float]
+    low_corner: Tuple[float, ...]
+    high_corner: Tuple[float, ...]
+    cell_size: Tuple[float, ...]
+
+    @property
+    def num_space_dim(self):
+        return len(self.low_corner)
 
     def extent(self, d):
         return self.high_corner[d] - self.low_corner[d]
@@ -67,24 +75,28 @@ def createUniformGlobalMesh(low_corner: Sequence[float], high_corner: Sequence[f
     """createUniformGlobalMesh for a scalar, per-dimension or cell-count argument.
 
     Mirrors the three GlobalMesh constructors (GlobalMesh.hpp:57-119): a scalar
-    or 3-sequence of floats is a cell size; a 3-sequence of ints is a cell
-    count. Raises ValueError where the reference throws std::logic_error.
+    or per-dimension sequence of floats is a cell size; a sequence of ints is
+    a cell count. Corners with 2 entries make a 2D mesh. Raises ValueError
+    where the reference throws std::logic_error.
     """
     low = tuple(float(v) for v in low_corner)
     high = tuple(float(v) for v in high_corner)
+    nd = len(low)
+    if nd not in (2, 3) or len(high) != nd:
+        raise ValueError("corners must both have 2 or 3 entries")
     if isinstance(cell_size, (int, float)) and not isinstance(cell_size, bool):
-        cs = (float(cell_size),) * 3
+        cs = (float(cell_size),) * nd
         counts = None
     else:
         vals = list(cell_size)
         if all(isinstance(v, int) for v in vals):
             counts = tuple(vals)
-            cs = tuple((high[d] - low[d]) / counts[d] for d in range(3))
+            cs = tuple((high[d] - low[d]) / counts[d] for d in range(nd))
         else:
             counts = None
             cs = tuple(float(v) for v in vals)
     mesh = GlobalMesh(low, high, cs)
-    for d in range(3):
+    for d in range(nd):
         ext = mesh.globalNumCell(d) * cs[d]
         if abs(ext - mesh.extent(d)) > 100.0 * _EPS:
             raise ValueError("Cabana::Grid::GlobalMesh: Extent not evenly divisible by uniform cell size")
@@ -98,7 +110,11 @@ class GlobalGrid:
     """One-rank GlobalGrid: the rank owns every cell (DimBlockPartitioner with a
     single block per dimension)."""
     global_mesh: GlobalMesh
-    periodic: Tuple[bool, bool, bool]
+    periodic: Tuple[bool, ...]
+
+    @property
+    def num_space_dim(self):
+        return self.global_mesh.num_space_dim
 
     def globalMesh(self):
         return self.global_mesh
@@ -113,7 +129,12 @@ class GlobalGrid:
         return 0
 
 
-def createGlobalGrid(global_mesh: GlobalMesh, is_dim_periodic=(False, False, False), partitioner=None, comm=None):
+def createGlobalGrid(global_mesh: GlobalMesh, is_dim_periodic=None, partitioner=None, comm=None):
+    nd = global_mesh.num_space_dim
+    if is_dim_periodic is None:
+        is_dim_periodic = (False,) * nd
+    if len(is_dim_periodic) != nd:
+        raise ValueError("one periodic flag per dimension")
     return GlobalGrid(global_mesh, tuple(bool(p) for p in is_dim_periodic))
 
 
@@ -121,6 +142,10 @@ def createGlobalGrid(global_mesh: GlobalMesh, is_dim_periodic=(False, False, Fal
 class LocalGrid:
     global_grid: GlobalGrid
     halo_cell_width: int
+
+    @property
+    def num_space_dim(self):
+        return self.global_grid.num_space_dim
 
     def globalGrid(self):
         return self.global_grid
@@ -134,14 +159,14 @@ class LocalGrid:
     def ghostedExtents(self, entity=NODE):
         """Extents of indexSpace(Ghost(), entity, Local())."""
         extra = 1 if entity == NODE else 0
-        return tuple(self.totalNumCell(d) + extra for d in range(3))
+        return tuple(self.totalNumCell(d) + extra for d in range(self.num_space_dim))
 
     def ownedSpace(self, entity=NODE):
         """[min, max) per dimension of indexSpace(Own(), entity, Local())
         (LocalGrid_impl.hpp:239-250, :430-450)."""
         out = []
         hw = self.halo_cell_width
-        for d in range(3):
+        for d in range(self.num_space_dim):
             nc = self.global_grid.ownedNumCell(d)
             if entity == NODE and not self.global_grid.isPeriodic(d):
                 out.append((hw, hw + nc + 1))
@@ -158,23 +183,25 @@ def createLocalGrid(global_grid: GlobalGrid, halo_cell_width: int) -> LocalGrid:
 class LocalMesh:
     """LocalMesh<UniformMesh> on one rank (LocalMesh.hpp:61-120)."""
     local_grid: LocalGrid
-    cell_size: Tuple[float, float, float] = field(init=False)
-    own_low: Tuple[float, float, float] = field(init=False)
-    ghost_low: Tuple[float, float, float] = field(init=False)
+    cell_size: Tuple[float, ...] = field(init=False)
+    own_low: Tuple[float, ...] = field(init=False)
+    ghost_low: Tuple[float, ...] = field(init=False)
 
     def __post_init__(self):
         gg = self.local_grid.global_grid
         gm = gg.global_mesh
-        self.cell_size = tuple(gm.cellSize(d) for d in range(3))
-        self.own_low = tuple(gm.lowCorner(d) + self.cell_size[d] * gg.globalOffset(d) for d in range(3))
+        nd = gm.num_space_dim
+        self.cell_size = tuple(gm.cellSize(d) for d in range(nd))
+        self.own_low = tuple(gm.lowCorner(d) + self.cell_size[d] * gg.globalOffset(d) for d in range(nd))
         hw = self.local_grid.halo_cell_width
-        self.ghost_low = tuple(self.own_low[d] - hw * self.cell_size[d] for d in range(3))
+        self.ghost_low = tuple(self.own_low[d] - hw * self.cell_size[d] for d in range(nd))
 
     def coordinates(self, entity, index):
         """coordinates(Node/Cell, index) (LocalMesh.hpp:180-200)."""
+        nd = len(self.cell_size)
         if entity == CELL:
-            return tuple(self.ghost_low[d] + (float(index[d]) + 0.5) * self.cell_size[d] for d in range(3))
-        return tuple(self.ghost_low[d] + float(index[d]) * self.cell_size[d] for d in range(3))
+            return tuple(self.ghost_low[d] + (float(index[d]) + 0.5) * self.cell_size[d] for d in range(nd))
+        return tuple(self.ghost_low[d] + float(index[d]) * self.cell_size[d] for d in range(nd))
 
 
 def createLocalMesh(local_grid: LocalGrid) -> LocalMesh:
@@ -183,29 +210,33 @@ def createLocalMesh(local_grid: LocalGrid) -> LocalMesh:
 
 @dataclass(frozen=True)
 class MeshParams:
-    """The scalars the kernels need; field for field the cgx_mesh struct."""
-    ghost_low: Tuple[float, float, float]
-    cell_size: Tuple[float, float, float]
-    owned_cells: Tuple[int, int, int]
+    """The scalars the kernels need; field for field the cgx_mesh struct
+    (per-dimension tuples have num_space_dim entries)."""
+    ghost_low: Tuple[float, ...]
+    cell_size: Tuple[float, ...]
+    owned_cells: Tuple[int, ...]
     halo_width: int
-    periodic: Tuple[int, int, int]
+    periodic: Tuple[int, ...]
     entity: int
+    num_space_dim: int = 3
 
     def extents(self):
         extra = 1 if self.entity == NODE else 0
-        return tuple(self.owned_cells[d] + 2 * self.halo_width + extra for d in range(3))
+        return tuple(self.owned_cells[d] + 2 * self.halo_width + extra for d in range(self.num_space_dim))
 
 
 def mesh_params(local_grid: LocalGrid, entity=NODE) -> MeshParams:
     lm = LocalMesh(local_grid)
     gg = local_grid.global_grid
+    nd = local_grid.num_space_dim
     return MeshParams(
         ghost_low=lm.ghost_low,
         cell_size=lm.cell_size,
-        owned_cells=tuple(gg.ownedNumCell(d) for d in range(3)),
+        owned_cells=tuple(gg.ownedNumCell(d) for d in range(nd)),
         halo_width=local_grid.halo_cell_width,
-        periodic=tuple(int(gg.isPeriodic(d)) for d in range(3)),
+        periodic=tuple(int(gg.isPeriodic(d)) for d in range(nd)),
         entity=int(entity),
+        num_space_dim=nd,
     )
 
 

@@ -88,6 +88,14 @@ typedef int cgx_status;
  * 61-120) plus the LocalGrid facts the halo needs
  * (grid/src/Cabana_Grid_LocalGrid_impl.hpp:49-60, :430-466).
  * Ghosted extents: owned_cells + 2*halo_width + (entity == CGX_NODE).
+ *
+ * num_space_dim 2 selects the 2D mesh (UniformMesh<double, 2>): entries [2]
+ * of the per-dimension members are ignored, points hold 2 coordinates, an
+ * Array is (i, j, dof), vector fields have 2 components and tensor fields
+ * 2 x 2 (the 2D specialisations of grid/src/Cabana_Grid_Interpolation.hpp:
+ * 81-98, :139-158, :212-237, :291-323, :373-396, :466-485, :527-547,
+ * :597-621, :674-702, :756-788). 2D runs the point kernels only (no tiling,
+ * adjoint or batched launches). 0 is read as 3.
  */
 typedef struct cgx_mesh {
     double ghost_low[3];     /* LocalMesh::lowCorner(Ghost(), d)            */
@@ -96,6 +104,8 @@ typedef struct cgx_mesh {
     int32_t halo_width;      /* LocalGrid::haloCellWidth()                  */
     int32_t periodic[3];     /* GlobalGrid::isPeriodic(d), one rank         */
     int32_t entity;          /* CGX_NODE / CGX_CELL of the arrays          */
+    int32_t num_space_dim;   /* 3 (or 0) or 2                               */
+    int32_t reserved;
 } cgx_mesh;
 
 /*

@@ -202,6 +202,9 @@ struct Spline3 {
     double d[3][kMaxKnot];
 };
 
+// Number of space dimensions of a mesh (num_space_dim 0 reads as 3).
+int dims(const oracle_mesh& m) { return m.num_space_dim == 2 ? 2 : 3; }
+
 void entity_coordinates(const oracle_mesh& m, int index, int dim, double& out) {
     if (m.entity == 1)  // Cell: ghost_low + (i + 0.5) * cell_size
         out = m.ghost_low[dim] + (double(index) + double(0.5)) * m.cell_size[dim];
@@ -209,30 +212,36 @@ void entity_coordinates(const oracle_mesh& m, int index, int dim, double& out) {
         out = m.ghost_low[dim] + double(index) * m.cell_size[dim];
 }
 
+// The point p holds dims(m) coordinates; in 2D the third dimension's
+// members are left zero.
 void evaluate(const oracle_mesh& m, int order, const double* p, Spline3& sd) {
+    const int nd = dims(m);
+    sd = Spline3{};
     sd.order = order;
     sd.nk = num_knot(order);
     double low_x[3], low_x_p1[3], rdx[3];
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < nd; ++d) {
         entity_coordinates(m, 0, d, low_x[d]);
         entity_coordinates(m, 1, d, low_x_p1[d]);
     }
-    for (int d = 0; d < 3; ++d) sd.dx[d] = low_x_p1[d] - low_x[d];
-    for (int d = 0; d < 3; ++d) rdx[d] = 1.0 / sd.dx[d];
-    for (int d = 0; d < 3; ++d) sd.x[d] = map_to_logical(order, p[d], rdx[d], low_x[d]);
-    for (int d = 0; d < 3; ++d) stencil(order, sd.x[d], sd.s[d]);
-    for (int d = 0; d < 3; ++d) value(order, sd.x[d], sd.w[d]);
-    for (int d = 0; d < 3; ++d) gradient(order, sd.x[d], rdx[d], sd.g[d]);
+    for (int d = 0; d < nd; ++d) sd.dx[d] = low_x_p1[d] - low_x[d];
+    for (int d = 0; d < nd; ++d) rdx[d] = 1.0 / sd.dx[d];
+    for (int d = 0; d < nd; ++d) sd.x[d] = map_to_logical(order, p[d], rdx[d], low_x[d]);
+    for (int d = 0; d < nd; ++d) stencil(order, sd.x[d], sd.s[d]);
+    for (int d = 0; d < nd; ++d) value(order, sd.x[d], sd.w[d]);
+    for (int d = 0; d < nd; ++d) gradient(order, sd.x[d], rdx[d], sd.g[d]);
     // SplinePhysicalDistance (Splines.hpp:1233-1251)
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < nd; ++d) {
         double offset = low_x[d] - p[d];
         for (int n = 0; n < sd.nk; ++n) sd.d[d][n] = offset + sd.s[d][n] * sd.dx[d];
     }
 }
 
+// Ghosted entity extents; a 2D mesh has one layer in the third dimension so
+// its (i, j, dof) arrays index as (i, j, 0, dof).
 void extents(const oracle_mesh& m, int64_t* ext) {
     for (int d = 0; d < 3; ++d)
-        ext[d] = int64_t(m.owned_cells[d]) + 2 * m.halo_width + (m.entity == 1 ? 0 : 1);
+        ext[d] = d < dims(m) ? int64_t(m.owned_cells[d]) + 2 * m.halo_width + (m.entity == 1 ? 0 : 1) : 1;
 }
 
 struct GridView {
@@ -245,8 +254,8 @@ struct GridView {
     }
 };
 
-bool stencil_in_range(const Spline3& sd, const int64_t* ext) {
-    for (int d = 0; d < 3; ++d) {
+bool stencil_in_range(const Spline3& sd, const int64_t* ext, int nd) {
+    for (int d = 0; d < nd; ++d) {
         if (sd.s[d][0] < 0 || sd.s[d][sd.nk - 1] >= ext[d]) return false;
     }
     return true;
@@ -324,19 +333,21 @@ void p2g_point(int kind, double mult, const double* xp, const Spline3& sd, GridV
     }
 }
 
-int p2g_comps(int kind) {
+// Components per point of each operator kind: scalars 1, vectors nd,
+// tensors nd * nd.
+int p2g_comps(int kind, int nd = 3) {
     switch (kind) {
         case 0: case 2: return 1;
-        case 1: case 3: return 3;
-        case 4: case 5: return 9;
+        case 1: case 3: return nd;
+        case 4: case 5: return nd * nd;
     }
     return -1;
 }
-int g2p_comps(int kind) {
+int g2p_comps(int kind, int nd = 3) {
     switch (kind) {
         case 0: case 4: return 1;
-        case 1: case 2: return 3;
-        case 3: case 5: return 9;
+        case 1: case 2: return nd;
+        case 3: case 5: return nd * nd;
     }
     return -1;
 }
@@ -417,6 +428,120 @@ void g2p_point(int kind, double mult, double* xp, const Spline3& sd, GridView& v
     }
 }
 
+// P2G:: thread-level operators, 2D specialisations (Interpolation.hpp:
+// 466-485, :527-547, :597-621, :674-702, :756-788); the functors premultiply
+// as in 3D.
+void p2g_point2(int kind, double mult, const double* xp, const Spline3& sd, GridView& v) {
+    const int nk = sd.nk;
+    switch (kind) {
+        case 0: {  // ScalarValueP2G -> P2G::value :466-485
+            double pd = xp[0] * mult;
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j) v.at(sd.s[0][i], sd.s[1][j], 0, 0) += pd * sd.w[0][i] * sd.w[1][j];
+            return;
+        }
+        case 1: {  // VectorValueP2G -> P2G::value :527-547
+            double pd[2];
+            for (int d = 0; d < 2; ++d) pd[d] = mult * xp[d];
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j)
+                    for (int d = 0; d < 2; ++d) v.at(sd.s[0][i], sd.s[1][j], 0, d) += pd[d] * sd.w[0][i] * sd.w[1][j];
+            return;
+        }
+        case 2: {  // ScalarGradientP2G -> P2G::gradient :597-621
+            double pd = xp[0] * mult;
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j) {
+                    v.at(sd.s[0][i], sd.s[1][j], 0, 0) += pd * sd.g[0][i] * sd.w[1][j];
+                    v.at(sd.s[0][i], sd.s[1][j], 0, 1) += pd * sd.w[0][i] * sd.g[1][j];
+                }
+            return;
+        }
+        case 3: {  // VectorDivergenceP2G -> P2G::divergence :674-702
+            double pd[2];
+            for (int d = 0; d < 2; ++d) pd[d] = mult * xp[d];
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j) {
+                    double result = pd[0] * sd.g[0][i] * sd.w[1][j] + pd[1] * sd.w[0][i] * sd.g[1][j];
+                    v.at(sd.s[0][i], sd.s[1][j], 0, 0) += result;
+                }
+            return;
+        }
+        case 4:    // TensorDivergenceP2G -> P2G::divergence :756-788
+        case 5: {  // the same on the transposed tensor
+            double pd[2][2];
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b) pd[a][b] = mult * (kind == 5 ? xp[b * 2 + a] : xp[a * 2 + b]);
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j) {
+                    double rg[2] = {sd.g[0][i] * sd.w[1][j], sd.w[0][i] * sd.g[1][j]};
+                    for (int d1 = 0; d1 < 2; ++d1)
+                        for (int d0 = 0; d0 < 2; ++d0) v.at(sd.s[0][i], sd.s[1][j], 0, d0) += rg[d1] * pd[d0][d1];
+                }
+            return;
+        }
+    }
+}
+
+// G2P:: thread-level operators, 2D specialisations (Interpolation.hpp:81-98,
+// :139-158, :212-237, :291-323, :373-396); x += multiplier * result.
+void g2p_point2(int kind, double mult, double* xp, const Spline3& sd, GridView& v) {
+    const int nk = sd.nk;
+    switch (kind) {
+        case 0: {  // ScalarValueG2P -> G2P::value :81-98
+            double result = 0.0;
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j) result += v.at(sd.s[0][i], sd.s[1][j], 0, 0) * sd.w[0][i] * sd.w[1][j];
+            xp[0] += mult * result;
+            return;
+        }
+        case 1: {  // VectorValueG2P -> G2P::value :139-158
+            double result[2] = {0.0, 0.0};
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j)
+                    for (int d = 0; d < 2; ++d)
+                        result[d] += v.at(sd.s[0][i], sd.s[1][j], 0, d) * sd.w[0][i] * sd.w[1][j];
+            for (int d = 0; d < 2; ++d) xp[d] += mult * result[d];
+            return;
+        }
+        case 2: {  // ScalarGradientG2P -> G2P::gradient :212-237
+            double result[2] = {0.0, 0.0};
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j) {
+                    double f = v.at(sd.s[0][i], sd.s[1][j], 0, 0);
+                    result[0] += f * sd.g[0][i] * sd.w[1][j];
+                    result[1] += f * sd.w[0][i] * sd.g[1][j];
+                }
+            for (int d = 0; d < 2; ++d) xp[d] += mult * result[d];
+            return;
+        }
+        case 3:    // VectorGradientG2P -> G2P::gradient :291-323 (result[m][n] = d_m W * f_n)
+        case 5: {  // the same stored transposed
+            double result[2][2] = {{0, 0}, {0, 0}};
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j) {
+                    double rg[2] = {sd.g[0][i] * sd.w[1][j], sd.w[0][i] * sd.g[1][j]};
+                    for (int d0 = 0; d0 < 2; ++d0) {
+                        double mg = rg[d0];
+                        for (int d1 = 0; d1 < 2; ++d1) result[d0][d1] += mg * v.at(sd.s[0][i], sd.s[1][j], 0, d1);
+                    }
+                }
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b) xp[kind == 5 ? b * 2 + a : a * 2 + b] += mult * result[a][b];
+            return;
+        }
+        case 4: {  // VectorDivergenceG2P -> G2P::divergence :373-396
+            double result = 0.0;
+            for (int i = 0; i < nk; ++i)
+                for (int j = 0; j < nk; ++j)
+                    result += v.at(sd.s[0][i], sd.s[1][j], 0, 0) * sd.g[0][i] * sd.w[1][j] +
+                              v.at(sd.s[0][i], sd.s[1][j], 0, 1) * sd.w[0][i] * sd.g[1][j];
+            xp[0] += result * mult;
+            return;
+        }
+    }
+}
+
 // Node/cell halo on a single rank (HaloBase.hpp:202-760 with the shared index
 // spaces of LocalGrid_impl.hpp:430-510). A ghost entity exchanges with an
 // owned one only when every dimension in which it lies outside the owned
@@ -424,6 +549,10 @@ void g2p_point(int kind, double mult, double* xp, const Spline3& sd, GridView& v
 bool halo_partner(const oracle_mesh& m, const int64_t* ext, const int64_t* idx, int64_t* own) {
     bool ghost = false;
     for (int d = 0; d < 3; ++d) {
+        if (d >= dims(m)) {  // the single layer of a 2D mesh
+            own[d] = idx[d];
+            continue;
+        }
         const int64_t hw = m.halo_width, nc = m.owned_cells[d];
         const int64_t own_hi = m.periodic[d] ? hw + nc : hw + nc + (m.entity == 1 ? 0 : 1);
         if (idx[d] >= hw && idx[d] < own_hi) {
@@ -515,16 +644,23 @@ int oracle_p2g(const oracle_mesh* mesh, const double* points, int64_t num_point,
                const oracle_op* ops, int n_ops, int nthreads) {
     int64_t ext[3];
     extents(*mesh, ext);
+    const int nd = dims(*mesh);
+    auto apply = [&](int o, int64_t p, const Spline3& sd, GridView& v) {
+        const double* xp = ops[o].x + p * p2g_comps(ops[o].kind, nd);
+        if (nd == 2)
+            p2g_point2(ops[o].kind, ops[o].multiplier, xp, sd, v);
+        else
+            p2g_point(ops[o].kind, ops[o].multiplier, xp, sd, v);
+    };
     int skipped = 0;
     if (nthreads <= 1) {
         std::vector<GridView> views;
         for (int o = 0; o < n_ops; ++o) views.push_back({ops[o].array, ext[0], ext[1], ext[2], ops[o].dofs});
         for (int64_t p = 0; p < num_point; ++p) {
             Spline3 sd;
-            evaluate(*mesh, order, points + 3 * p, sd);
-            if (!stencil_in_range(sd, ext)) { ++skipped; continue; }
-            for (int o = 0; o < n_ops; ++o)
-                p2g_point(ops[o].kind, ops[o].multiplier, ops[o].x + p * p2g_comps(ops[o].kind), sd, views[o]);
+            evaluate(*mesh, order, points + nd * p, sd);
+            if (!stencil_in_range(sd, ext, nd)) { ++skipped; continue; }
+            for (int o = 0; o < n_ops; ++o) apply(o, p, sd, views[o]);
         }
     } else {
 #ifdef _OPENMP
@@ -545,10 +681,9 @@ int oracle_p2g(const oracle_mesh* mesh, const double* points, int64_t num_point,
             #pragma omp for schedule(static)
             for (int64_t p = 0; p < num_point; ++p) {
                 Spline3 sd;
-                evaluate(*mesh, order, points + 3 * p, sd);
-                if (!stencil_in_range(sd, ext)) { ++skipped; continue; }
-                for (int o = 0; o < n_ops; ++o)
-                    p2g_point(ops[o].kind, ops[o].multiplier, ops[o].x + p * p2g_comps(ops[o].kind), sd, views[o]);
+                evaluate(*mesh, order, points + nd * p, sd);
+                if (!stencil_in_range(sd, ext, nd)) { ++skipped; continue; }
+                for (int o = 0; o < n_ops; ++o) apply(o, p, sd, views[o]);
             }
             #pragma omp barrier
             for (int o = 0; o < n_ops; ++o) {
@@ -577,6 +712,7 @@ int oracle_g2p(const oracle_mesh* mesh, const double* points, int64_t num_point,
                const oracle_op* ops, int n_ops, int nthreads) {
     int64_t ext[3];
     extents(*mesh, ext);
+    const int nd = dims(*mesh);
     for (int o = 0; o < n_ops; ++o) {
         bool seen = false;
         for (int q = 0; q < o; ++q) seen |= (ops[q].array == ops[o].array);
@@ -590,11 +726,15 @@ int oracle_g2p(const oracle_mesh* mesh, const double* points, int64_t num_point,
 #endif
     for (int64_t p = 0; p < num_point; ++p) {
         Spline3 sd;
-        evaluate(*mesh, order, points + 3 * p, sd);
-        if (!stencil_in_range(sd, ext)) { ++skipped; continue; }
+        evaluate(*mesh, order, points + nd * p, sd);
+        if (!stencil_in_range(sd, ext, nd)) { ++skipped; continue; }
         for (int o = 0; o < n_ops; ++o) {
             GridView v = views[o];
-            g2p_point(ops[o].kind, ops[o].multiplier, ops[o].x + p * g2p_comps(ops[o].kind), sd, v);
+            double* xp = ops[o].x + p * g2p_comps(ops[o].kind, nd);
+            if (nd == 2)
+                g2p_point2(ops[o].kind, ops[o].multiplier, xp, sd, v);
+            else
+                g2p_point(ops[o].kind, ops[o].multiplier, xp, sd, v);
         }
     }
     return skipped;
@@ -749,8 +889,10 @@ void oracle_stable_sort_keys(const uint64_t* keys, int64_t n, uint64_t* permutes
 // (ghost += owned image) is applied to it first, in place.
 int oracle_p2g_adjoint(const oracle_mesh* mesh, const double* points, int64_t num_point, int order,
                        const oracle_adjoint_op* ops, int n_ops, double* points_bar) {
+    if (dims(*mesh) != 3) return -1;  // the adjoints are written for 3D meshes
     int64_t ext[3];
     extents(*mesh, ext);
+    const int nd = 3;
     for (int o = 0; o < n_ops; ++o) {
         bool seen = false;
         for (int q = 0; q < o; ++q) seen |= (ops[q].array_bar == ops[o].array_bar);
@@ -760,7 +902,7 @@ int oracle_p2g_adjoint(const oracle_mesh* mesh, const double* points, int64_t nu
     for (int64_t p = 0; p < num_point; ++p) {
         Spline3 sd;
         evaluate(*mesh, order, points + 3 * p, sd);
-        if (!stencil_in_range(sd, ext)) { ++skipped; continue; }
+        if (!stencil_in_range(sd, ext, nd)) { ++skipped; continue; }
         double h[3][kMaxKnot];
         for (int d = 0; d < 3; ++d) hessian(order, sd.x[d], 1.0 / sd.dx[d], h[d]);
         double pos[3] = {0.0, 0.0, 0.0};
@@ -826,13 +968,15 @@ int oracle_p2g_adjoint(const oracle_mesh* mesh, const double* points, int64_t nu
 // += ghost, ghost = 0) is applied to it afterwards.
 int oracle_g2p_adjoint(const oracle_mesh* mesh, const double* points, int64_t num_point, int order,
                        const oracle_adjoint_op* ops, int n_ops, double* points_bar) {
+    if (dims(*mesh) != 3) return -1;  // the adjoints are written for 3D meshes
     int64_t ext[3];
     extents(*mesh, ext);
+    const int nd = 3;
     int skipped = 0;
     for (int64_t p = 0; p < num_point; ++p) {
         Spline3 sd;
         evaluate(*mesh, order, points + 3 * p, sd);
-        if (!stencil_in_range(sd, ext)) { ++skipped; continue; }
+        if (!stencil_in_range(sd, ext, nd)) { ++skipped; continue; }
         double h[3][kMaxKnot];
         for (int d = 0; d < 3; ++d) hessian(order, sd.x[d], 1.0 / sd.dx[d], h[d]);
         double pos[3] = {0.0, 0.0, 0.0};

@@ -40,6 +40,8 @@ typedef struct oracle_mesh {
     int32_t halo_width;
     int32_t periodic[3];
     int32_t entity;  // 0 = Node, 1 = Cell
+    int32_t num_space_dim;  // 3 (or 0) or 2: entries [2] are then ignored
+    int32_t reserved;
 } oracle_mesh;
 
 // One operator. `x` is a dense row-major (num_point, comps) double array,

@@ -6,7 +6,9 @@ this module.
 
 Arrays are plain numpy float64 arrays: points ``(n, 3)``, particle fields
 ``(n, comps)`` and grid arrays ``(ni, nj, nk, dofs)`` in C order, which is the
-reference's LayoutRight ``Array`` layout.
+reference's LayoutRight ``Array`` layout. On a 2D mesh (``make_mesh(...,
+num_space_dim=2)``) points are ``(n, 2)``, vectors have 2 components, tensors
+4, and grid arrays are ``(ni, nj, dofs)``.
 """
 import ctypes
 import os
@@ -23,6 +25,10 @@ P2G_COMPS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 9, 5: 9}
 P2G_DOFS = {0: 1, 1: 3, 2: 3, 3: 1, 4: 3, 5: 3}
 G2P_COMPS = {0: 1, 1: 3, 2: 3, 3: 9, 4: 1, 5: 9}
 G2P_DOFS = {0: 1, 1: 3, 2: 1, 3: 3, 4: 3, 5: 3}
+P2G_COMPS_2D = {0: 1, 1: 2, 2: 1, 3: 2, 4: 4, 5: 4}
+P2G_DOFS_2D = {0: 1, 1: 2, 2: 2, 3: 1, 4: 2, 5: 2}
+G2P_COMPS_2D = {0: 1, 1: 2, 2: 2, 3: 4, 4: 1, 5: 4}
+G2P_DOFS_2D = {0: 1, 1: 2, 2: 1, 3: 2, 4: 2, 5: 2}
 
 
 class OracleMesh(ctypes.Structure):
@@ -33,6 +39,8 @@ class OracleMesh(ctypes.Structure):
         ("halo_width", ctypes.c_int32),
         ("periodic", ctypes.c_int32 * 3),
         ("entity", ctypes.c_int32),
+        ("num_space_dim", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 
@@ -95,22 +103,28 @@ def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
 
 
-def make_mesh(ghost_low, cell_size, owned_cells, halo_width, periodic=(0, 0, 0), entity=0):
+def make_mesh(ghost_low, cell_size, owned_cells, halo_width, periodic=(0, 0, 0), entity=0, num_space_dim=3):
+    """Per-dimension arguments have num_space_dim entries (3 or 2)."""
     m = OracleMesh()
-    for d in range(3):
+    for d in range(num_space_dim):
         m.ghost_low[d] = float(ghost_low[d])
         m.cell_size[d] = float(cell_size[d])
         m.owned_cells[d] = int(owned_cells[d])
         m.periodic[d] = int(bool(periodic[d]))
+    for d in range(num_space_dim, 3):
+        m.cell_size[d] = 1.0
+        m.owned_cells[d] = 1
     m.halo_width = int(halo_width)
     m.entity = int(entity)
+    m.num_space_dim = int(num_space_dim)
     return m
 
 
 def extents(mesh):
+    """Ghosted entity extents: 3 values, or 2 on a 2D mesh."""
     ext = np.zeros(3, np.int64)
     lib().oracle_extents(ctypes.byref(mesh), ext.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
-    return tuple(int(e) for e in ext)
+    return tuple(int(e) for e in ext[:2 if mesh.num_space_dim == 2 else 3])
 
 
 def num_knot(order):
@@ -172,7 +186,7 @@ def _ops(ops, n, comps_table):
         assert array.dtype == np.float64 and array.flags.c_contiguous
         assert x.reshape(n, -1).shape[1] == comps_table[kind]
         arr[i].kind = kind
-        arr[i].dofs = array.shape[3]
+        arr[i].dofs = array.shape[-1]
         arr[i].multiplier = float(mult)
         arr[i].x = _dp(x)
         arr[i].array = _dp(array)
@@ -184,7 +198,7 @@ def p2g(mesh, points, order, ops, nthreads=1):
     """ops: list of (kind, multiplier, x, array); arrays are updated in place."""
     points = np.ascontiguousarray(points, np.float64)
     n = points.shape[0]
-    arr, _keep = _ops(ops, n, P2G_COMPS)
+    arr, _keep = _ops(ops, n, P2G_COMPS_2D if mesh.num_space_dim == 2 else P2G_COMPS)
     return lib().oracle_p2g(ctypes.byref(mesh), _dp(points), n, order, arr, len(ops), nthreads)
 
 
@@ -192,7 +206,7 @@ def g2p(mesh, points, order, ops, nthreads=1):
     """ops: list of (kind, multiplier, x, array); particle fields x are updated in place."""
     points = np.ascontiguousarray(points, np.float64)
     n = points.shape[0]
-    arr, _keep = _ops(ops, n, G2P_COMPS)
+    arr, _keep = _ops(ops, n, G2P_COMPS_2D if mesh.num_space_dim == 2 else G2P_COMPS)
     return lib().oracle_g2p(ctypes.byref(mesh), _dp(points), n, order, arr, len(ops), nthreads)
 
 
@@ -231,11 +245,11 @@ def g2p_adjoint(mesh, points, order, ops, points_bar=None):
 
 
 def halo_scatter_sum(mesh, array):
-    lib().oracle_halo_scatter_sum(ctypes.byref(mesh), _dp(array), ctypes.c_int(array.shape[3]))
+    lib().oracle_halo_scatter_sum(ctypes.byref(mesh), _dp(array), ctypes.c_int(array.shape[-1]))
 
 
 def halo_gather(mesh, array):
-    lib().oracle_halo_gather(ctypes.byref(mesh), _dp(array), ctypes.c_int(array.shape[3]))
+    lib().oracle_halo_gather(ctypes.byref(mesh), _dp(array), ctypes.c_int(array.shape[-1]))
 
 
 def cartesian_num_bins(grid_min, grid_max, grid_delta):

@@ -99,3 +99,13 @@ def test_argument_checks_fail_loudly(lib):
     t = L.CgxTiling()
     assert lib.cgx_tiling_init(ctypes.byref(bad), 2, (ctypes.c_int32 * 3)(8, 8, 8), ctypes.byref(t)) == L.CGX_ERR_INVALID_ARG
     assert lib.cgx_tiling_init(ctypes.byref(mesh), 9, (ctypes.c_int32 * 3)(8, 8, 8), ctypes.byref(t)) == L.CGX_ERR_NOT_SUPPORTED
+    # 2D meshes: accepted by the interpolation entry points, refused by the
+    # 3D-only tiling; other dimension counts are refused
+    gm2 = M.createUniformGlobalMesh((0.0, 0.0), (2.0, 3.0), 0.5)
+    mesh2 = L.make_mesh(M.mesh_params(M.createLocalGrid(M.createGlobalGrid(gm2), 1)))
+    assert mesh2.num_space_dim == 2 and mesh2.owned_cells[2] == 1
+    assert lib.cgx_tiling_init(ctypes.byref(mesh2), 2, (ctypes.c_int32 * 3)(8, 8, 8), ctypes.byref(t)) == L.CGX_ERR_NOT_SUPPORTED
+    assert b"3D" in lib.cgx_last_error()
+    mesh4 = L.make_mesh(mp)
+    mesh4.num_space_dim = 4
+    assert lib.cgx_tiling_init(ctypes.byref(mesh4), 2, (ctypes.c_int32 * 3)(8, 8, 8), ctypes.byref(t)) == L.CGX_ERR_INVALID_ARG
