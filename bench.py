@@ -616,42 +616,82 @@ def run_ours(args):
         del ref
         torch.cuda.empty_cache()
 
-    # ---- end to end through the C ABI with pinned host buffers
+    # ---- end to end through the C ABI with pinned host buffers. Every step
+    # copies its inputs in (H2D), tile-sorts and permutes them, runs P2G + G2P
+    # and copies its results out (D2H). Steps are pipelined the way a
+    # streaming caller runs them: two device buffer sets, one stream each for
+    # H2D, compute and D2H, so step k+1's inputs cross the host link while
+    # step k computes and step k-1's results travel back (a third set
+    # measured no faster: the host link is the bound).
     e2e = None
     if not args.no_e2e:
         h_in = [t.cpu().pin_memory() for t in (pos, mass, mom, stress)]
-        h_out = [torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in (tr.vel, tr.velgrad)]
         h2d = sum(t.numel() * t.element_size() for t in h_in)
-        d2h = sum(t.numel() * t.element_size() for t in h_out)
+        nsets = 2
+        sets = [tr]
+        for _ in range(nsets - 1):
+            bufs = [torch.empty_like(t) for t in (pos, mass, mom, stress)]
+            sets.append(Transfer(G, lg, *bufs, torch.float32, G.FP32_COMPENSATED, tiling))
+        h_out = [[torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in (ts.vel, ts.velgrad)] for ts in sets]
+        d2h = sum(t.numel() * t.element_size() for t in h_out[0])
+        s_in, s_cmp, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        ev = lambda: torch.cuda.Event()  # noqa: E731
+        pos_ready = [ev() for _ in range(nsets)]
+        in_ready = [ev() for _ in range(nsets)]
+        cmp_done = [ev() for _ in range(nsets)]
+        out_read = [ev() for _ in range(nsets)]
 
-        def e2e_step():
-            for hd, dd in zip(h_in, (pos, mass, mom, stress)):
-                dd.copy_(hd, non_blocking=True)
-            # the caller's particles arrive in any order: tile-sort and permute them every step
-            C.permute_by(tiling.sort(pos, n), pos, mass, mom, stress)
-            tr.zero(); tr.vel.zero_(); tr.velgrad.zero_(); tr.p2g(); tr.g2p()
-            h_out[0].copy_(tr.vel, non_blocking=True)
-            h_out[1].copy_(tr.velgrad, non_blocking=True)
+        def e2e_step(k):
+            sidx = k % nsets
+            ts = sets[sidx]
+            dev_in = (ts.pos,) + tuple(f.x for f in ts.p2g_f)
+            with torch.cuda.stream(s_in):
+                s_in.wait_event(cmp_done[sidx])  # the set's last compute has read its inputs
+                for j, (hd, dd) in enumerate(zip(h_in, dev_in)):
+                    dd.copy_(hd, non_blocking=True)
+                    if j == 0:
+                        pos_ready[sidx].record(s_in)
+                in_ready[sidx].record(s_in)
+            with torch.cuda.stream(s_cmp):
+                s_cmp.wait_event(pos_ready[sidx])
+                # the caller's particles arrive in any order: tile-sort and permute them every step
+                perm = tiling.sort(ts.pos, n)
+                s_cmp.wait_event(in_ready[sidx])
+                C.permute_by(perm, *dev_in)
+                s_cmp.wait_event(out_read[sidx])  # the set's last results have been read back
+                ts.zero(); ts.vel.zero_(); ts.velgrad.zero_(); ts.p2g(); ts.g2p()
+                cmp_done[sidx].record(s_cmp)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(cmp_done[sidx])
+                h_out[sidx][0].copy_(ts.vel, non_blocking=True)
+                h_out[sidx][1].copy_(ts.velgrad, non_blocking=True)
+                out_read[sidx].record(s_out)
 
-        for _ in range(max(1, args.warmup // 2)):
-            e2e_step()
-        esteps = max(2, min(args.steps, 5))
+        for k in range(max(nsets, args.warmup)):
+            e2e_step(k)
+        esteps = max(6, min(args.steps, 9))
         torch.cuda.synchronize()
         barrier()
         s0 = torch.cuda.Event(enable_timing=True)
         s1 = torch.cuda.Event(enable_timing=True)
-        s0.record()
-        for _ in range(esteps):
-            e2e_step()
-        s1.record()
+        s0.record(s_in)
+        for k in range(esteps):
+            e2e_step(k)
+        s1.record(s_out)
         torch.cuda.synchronize()
         barrier()
         ems = s0.elapsed_time(s1) / esteps
+        # every buffer set processed the same inputs: their last results agree
+        # up to the summation order of the grid atomics
+        sets_rel = max(float((h_out[i][j] - h_out[0][j]).abs().max() / h_out[0][j].abs().max())
+                       for i in range(1, nsets) for j in range(2))
         e2e = {"value": n * world / (ems / 1000.0), "unit": "particles/s", "ms_per_step": ems,
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "buffer_sets_max_rel": sets_rel,
                "note": "pinned host buffers; every step: H2D of positions, mass, momentum, stress, tile sort + "
-                       "permute of all particle fields, zero grids, P2G + G2P, D2H of velocity and velocity gradient"}
-        del h_in, h_out
+                       "permute of all particle fields, zero grids, P2G + G2P, D2H of velocity and velocity "
+                       "gradient; steps pipelined over two device buffer sets (H2D, compute and D2H streams)"}
+        del h_in, h_out, sets
+        torch.cuda.empty_cache()
 
     batched = None
     if rank == 0 and not args.no_batch:
