@@ -38,7 +38,7 @@ CGX_DISPATCH_TILED = 2
 
 EXPORTS = (
     "cgx_create", "cgx_destroy", "cgx_last_error", "cgx_version", "cgx_last_dispatch",
-    "cgx_p2g", "cgx_g2p", "cgx_p2g_adjoint", "cgx_g2p_adjoint", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
+    "cgx_p2g", "cgx_g2p", "cgx_g2p2g", "cgx_p2g_adjoint", "cgx_g2p_adjoint", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
     "cgx_cartesian_num_bins", "cgx_linked_cell_build", "cgx_bin_by_key", "cgx_bin_by_key_static", "cgx_permute",
     "cgx_tiling_init", "cgx_tiling_num_offsets", "cgx_sort_tiles",
     "cgx_batch_plan_create", "cgx_batch_plan_destroy", "cgx_batch_execute", "cgx_batch_autotune",
@@ -152,6 +152,8 @@ def lib():
               P(CgxTiling), ctypes.c_uint, vp]
     L.cgx_p2g.argtypes = interp
     L.cgx_g2p.argtypes = interp
+    L.cgx_g2p2g.argtypes = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, ctypes.c_int, P(CgxOp), ctypes.c_int, P(CgxOp),
+                            ctypes.c_int, ctypes.c_int, ctypes.c_uint, vp]
     adj = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, ctypes.c_int, P(CgxAdjointOp), ctypes.c_int, ctypes.c_int,
            P(CgxTiling), P(CgxField), ctypes.c_uint, vp]
     L.cgx_p2g_adjoint.argtypes = adj

@@ -773,6 +773,98 @@ cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, 
     return interpolate(h, mesh, points, num_point, spline_order, ops, n_ops, precision, tiling, flags, stream, false);
 }
 
+cgx_status cgx_g2p2g(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point, int spline_order,
+                     const cgx_op* g2p_ops, int n_g2p, const cgx_op* p2g_ops, int n_p2g, int precision, unsigned flags,
+                     void* stream) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    cgx_status s = check_mesh(mesh);
+    if (s) return s;
+    if (mesh_dims(*mesh) != 3) return fail(CGX_ERR_NOT_SUPPORTED, "g2p2g is built for 3D meshes");
+    if (num_point < 0) return fail(CGX_ERR_INVALID_ARG, "num_point must be >= 0");
+    if (num_point > 0) {
+        s = check_field(points, "points");
+        if (s) return s;
+        if (points->dtype != CGX_F64) return fail(CGX_ERR_INVALID_ARG, "point coordinates must be double (CGX_F64)");
+    }
+    if (spline_order < 0 || spline_order > 6) return fail(CGX_ERR_NOT_SUPPORTED, "spline order must be in [0, 6]");
+    if (precision != CGX_PLAIN_FP64 && precision != CGX_FP32_COMPENSATED)
+        return fail(CGX_ERR_INVALID_ARG, "unknown precision");
+    if (n_g2p < 1 || n_p2g < 1 || n_g2p + n_p2g > kMaxOps)
+        return fail(CGX_ERR_INVALID_ARG, "g2p2g takes >= 1 G2P and >= 1 P2G functor, 8 in all");
+    s = check_ops(g2p_ops, n_g2p, false, num_point > 0);
+    if (s) return s;
+    s = check_ops(p2g_ops, n_p2g, true, num_point > 0);
+    if (s) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (flags & CGX_FLAG_CHECK_BOUNDS) CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
+    if (!(flags & CGX_FLAG_SKIP_HALO)) {
+        s = halo_all(*mesh, g2p_ops, n_g2p, kHaloGather, h->sms, st);
+        if (s) return s;
+    }
+    const DMesh dm = to_dmesh(*mesh);
+    const int64_t nodes = int64_t(dm.ext[0]) * dm.ext[1] * dm.ext[2];
+    // G2P reads each array as it was at the call: an array that a P2G functor
+    // also writes is read from a snapshot in the workspace.
+    std::vector<cgx_op> gops(g2p_ops, g2p_ops + n_g2p);
+    std::vector<size_t> snap_off(n_g2p, size_t(-1));
+    size_t snap_bytes = 0;
+    for (int o = 0; o < n_g2p; ++o) {
+        bool written = false;
+        for (int q = 0; q < n_p2g; ++q) written |= p2g_ops[q].array.data == gops[o].array.data;
+        if (!written) continue;
+        for (int q = 0; q < o; ++q)
+            if (g2p_ops[q].array.data == gops[o].array.data) snap_off[o] = snap_off[q];
+        if (snap_off[o] != size_t(-1)) continue;
+        snap_off[o] = snap_bytes;
+        const size_t bytes = size_t(nodes) * gops[o].array.dofs * (gops[o].array.dtype == CGX_F64 ? 8 : 4);
+        snap_bytes += (bytes + 255) / 256 * 256;
+    }
+    if (snap_bytes > 0 && num_point > 0) {
+        s = ensure_ws(h, snap_bytes);
+        if (s) return s;
+        for (int o = 0; o < n_g2p; ++o) {
+            if (snap_off[o] == size_t(-1)) continue;
+            char* snap = reinterpret_cast<char*>(h->ws) + snap_off[o];
+            bool first = true;
+            for (int q = 0; q < o; ++q) first &= snap_off[q] != snap_off[o];
+            if (first) {
+                const size_t bytes = size_t(nodes) * gops[o].array.dofs * (gops[o].array.dtype == CGX_F64 ? 8 : 4);
+                CGX_CUDA(cudaMemcpyAsync(snap, gops[o].array.data, bytes, cudaMemcpyDeviceToDevice, st));
+            }
+            gops[o].array.data = snap;
+        }
+    }
+    if (num_point > 0) {
+        PointParams prm;
+        std::memset(&prm, 0, sizeof(prm));
+        prm.mesh = dm;
+        prm.points = to_dfield(*points);
+        prm.num_point = num_point;
+        prm.n_ops = n_g2p + n_p2g;
+        prm.n_g2p = n_g2p;
+        prm.dims = 3;
+        prm.error_flag = h->flags;
+        for (int o = 0; o < prm.n_ops; ++o) {
+            const cgx_op& op = o < n_g2p ? gops[o] : p2g_ops[o - n_g2p];
+            prm.ops[o].kind = op.kind;
+            prm.ops[o].slot = o;
+            prm.ops[o].mult = op.multiplier;
+            prm.ops[o].mult_f = float(op.multiplier);
+            prm.ops[o].x = to_dfield(op.x);
+            prm.ops[o].a.data = reinterpret_cast<char*>(op.array.data);
+            prm.ops[o].a.dtype = op.array.dtype;
+            prm.ops[o].a.dofs = op.array.dofs;
+        }
+        CGX_CUDA(launch_g2p2g_points(prm, spline_order, precision == CGX_PLAIN_FP64, h->sms, st));
+        h->last_dispatch = CGX_DISPATCH_POINTS;
+    }
+    if (!(flags & CGX_FLAG_SKIP_HALO)) {
+        s = halo_all(*mesh, p2g_ops, n_p2g, kHaloScatterSum, h->sms, st);
+        if (s) return s;
+    }
+    return finish_check(h, flags, st);
+}
+
 cgx_status cgx_p2g_adjoint(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point,
                            int spline_order, const cgx_adjoint_op* ops, int n_ops, int precision,
                            const cgx_tiling* tiling, const cgx_field* points_bar, unsigned flags, void* stream) {

@@ -11,6 +11,8 @@ struct PointParams {
     int64_t num_point;
     int32_t n_ops;
     int32_t dims;  // 3, or 2 for a 2D mesh (mesh.ext[2] == 1; points hold 2 coordinates)
+    int32_t n_g2p;  // fused g2p2g: ops[0, n_g2p) are G2P, the rest P2G
+    int32_t reserved;
     int* error_flag;
     DOp ops[kMaxOps];
 };
@@ -166,6 +168,8 @@ enum HaloMode : int {
 };
 
 cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64, int sms, cudaStream_t st);
+// Fused g2p2g on the point kernels (3D): ops[0, prm.n_g2p) G2P, then P2G.
+cudaError_t launch_g2p2g_points(const PointParams& prm, int order, bool fp64, int sms, cudaStream_t st);
 cudaError_t launch_adjoint_points(const AdjointParams& prm, int order, bool fp64, int sms, cudaStream_t st);
 cudaError_t launch_halo(const HaloParams& h, int mode, int sms, cudaStream_t st);
 cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st);

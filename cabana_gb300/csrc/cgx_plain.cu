@@ -11,253 +11,282 @@
 
 namespace cgx {
 
+// Spline weights of point p on a 3D mesh (the SplineData of evaluateSpline,
+// grid/src/Cabana_Grid_Splines.hpp:1280-1342); false when the stencil leaves
+// the ghosted index space.
 template <int ORDER, class T>
-__global__ void __launch_bounds__(256) p2g_points_kernel(const __grid_constant__ PointParams prm) {
+__device__ __forceinline__ bool weights_3d(const PointParams& prm, int64_t p, int* s, T (*w)[ORDER + 1],
+                                           T (*g)[ORDER + 1]) {
     using S = SplineKernel<ORDER, T>;
     constexpr int nk = S::nk;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double xp = load_field<double>(prm.points, p, d);
+        const double x0 = logical_coord<ORDER>(xp, prm.mesh.low[d], prm.mesh.rdx[d]);
+        T u;
+        base_and_offset<ORDER, T>(x0, s[d], u);
+        ok &= (x0 >= 0.0) && (s[d] >= 0) && (s[d] + nk <= prm.mesh.ext[d]);
+        if constexpr (sizeof(T) == 8)
+            S::weights(u, prm.mesh.rdx[d], w[d], g[d]);
+        else
+            S::weights(u, prm.mesh.rdx_f[d], w[d], g[d]);
+    }
+    return ok;
+}
+
+// One P2G functor on point p (the functor bodies of Interpolation.hpp:
+// 1324-1566 over P2G::value / gradient / divergence, :437-747), atomically.
+template <int ORDER, class T>
+__device__ __forceinline__ void p2g_apply(const PointParams& prm, const DOp& op, int64_t p, const int* s,
+                                          const T (*w)[ORDER + 1], const T (*g)[ORDER + 1]) {
+    constexpr int nk = ORDER + 1;
     constexpr int U = ORDER <= 3 ? nk : 1;  // full unroll only for the hot orders
-    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < prm.num_point; p += stride) {
-        int s[3];
-        T w[3][nk], g[3][nk];
-        bool ok = true;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const double xp = load_field<double>(prm.points, p, d);
-            const double x0 = logical_coord<ORDER>(xp, prm.mesh.low[d], prm.mesh.rdx[d]);
-            T u;
-            base_and_offset<ORDER, T>(x0, s[d], u);
-            ok &= (x0 >= 0.0) && (s[d] >= 0) && (s[d] + nk <= prm.mesh.ext[d]);
-            if constexpr (sizeof(T) == 8)
-                S::weights(u, prm.mesh.rdx[d], w[d], g[d]);
-            else
-                S::weights(u, prm.mesh.rdx_f[d], w[d], g[d]);
+    const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
+    switch (op.kind) {
+        case CGX_SCALAR_VALUE_P2G: {
+            const T pd = load_field<T>(op.x, p, 0) * mult;
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j)
+#pragma unroll U
+                    for (int k = 0; k < nk; ++k)
+                        atomic_add_array(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0,
+                                         pd * w[0][i] * w[1][j] * w[2][k]);
+            break;
         }
-        if (!ok) {
-            raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
-            continue;
+        case CGX_VECTOR_VALUE_P2G: {
+            T pd[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) pd[d] = mult * load_field<T>(op.x, p, d);
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j)
+#pragma unroll U
+                    for (int k = 0; k < nk; ++k) {
+                        const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+                        const T wijk = w[0][i] * w[1][j] * w[2][k];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) atomic_add_array(op.a, n, d, pd[d] * wijk);
+                    }
+            break;
         }
-        for (int o = 0; o < prm.n_ops; ++o) {
-            const DOp& op = prm.ops[o];
-            const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
-            switch (op.kind) {
-                case CGX_SCALAR_VALUE_P2G: {
-                    const T pd = load_field<T>(op.x, p, 0) * mult;
+        case CGX_SCALAR_GRADIENT_P2G: {
+            const T pd = load_field<T>(op.x, p, 0) * mult;
 #pragma unroll U
-                    for (int i = 0; i < nk; ++i)
+            for (int i = 0; i < nk; ++i)
 #pragma unroll U
-                        for (int j = 0; j < nk; ++j)
+                for (int j = 0; j < nk; ++j)
 #pragma unroll U
-                            for (int k = 0; k < nk; ++k)
-                                atomic_add_array(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0,
-                                                 pd * w[0][i] * w[1][j] * w[2][k]);
-                    break;
-                }
-                case CGX_VECTOR_VALUE_P2G: {
-                    T pd[3];
+                    for (int k = 0; k < nk; ++k) {
+                        const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+                        atomic_add_array(op.a, n, 0, pd * g[0][i] * w[1][j] * w[2][k]);
+                        atomic_add_array(op.a, n, 1, pd * w[0][i] * g[1][j] * w[2][k]);
+                        atomic_add_array(op.a, n, 2, pd * w[0][i] * w[1][j] * g[2][k]);
+                    }
+            break;
+        }
+        case CGX_VECTOR_DIVERGENCE_P2G: {
+            T pd[3];
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) pd[d] = mult * load_field<T>(op.x, p, d);
+            for (int d = 0; d < 3; ++d) pd[d] = mult * load_field<T>(op.x, p, d);
 #pragma unroll U
-                    for (int i = 0; i < nk; ++i)
+            for (int i = 0; i < nk; ++i)
 #pragma unroll U
-                        for (int j = 0; j < nk; ++j)
+                for (int j = 0; j < nk; ++j)
 #pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
-                                const T wijk = w[0][i] * w[1][j] * w[2][k];
+                    for (int k = 0; k < nk; ++k) {
+                        const T r = pd[0] * g[0][i] * w[1][j] * w[2][k] + pd[1] * w[0][i] * g[1][j] * w[2][k] +
+                                    pd[2] * w[0][i] * w[1][j] * g[2][k];
+                        atomic_add_array(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0, r);
+                    }
+            break;
+        }
+        case CGX_TENSOR_DIVERGENCE_P2G:
+        case CGX_TENSOR_DIVERGENCE_T_P2G: {
+            // pd[m][n]: the tensor entry paired with dW/dx_n for grid dof m
+            const bool tr = op.kind == CGX_TENSOR_DIVERGENCE_T_P2G;
+            T pd[3][3];
 #pragma unroll
-                                for (int d = 0; d < 3; ++d) atomic_add_array(op.a, n, d, pd[d] * wijk);
-                            }
-                    break;
-                }
-                case CGX_SCALAR_GRADIENT_P2G: {
-                    const T pd = load_field<T>(op.x, p, 0) * mult;
-#pragma unroll U
-                    for (int i = 0; i < nk; ++i)
-#pragma unroll U
-                        for (int j = 0; j < nk; ++j)
-#pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
-                                atomic_add_array(op.a, n, 0, pd * g[0][i] * w[1][j] * w[2][k]);
-                                atomic_add_array(op.a, n, 1, pd * w[0][i] * g[1][j] * w[2][k]);
-                                atomic_add_array(op.a, n, 2, pd * w[0][i] * w[1][j] * g[2][k]);
-                            }
-                    break;
-                }
-                case CGX_VECTOR_DIVERGENCE_P2G: {
-                    T pd[3];
+            for (int a = 0; a < 3; ++a)
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) pd[d] = mult * load_field<T>(op.x, p, d);
+                for (int b = 0; b < 3; ++b) pd[a][b] = mult * load_field<T>(op.x, p, tr ? b * 3 + a : a * 3 + b);
 #pragma unroll U
-                    for (int i = 0; i < nk; ++i)
+            for (int i = 0; i < nk; ++i)
 #pragma unroll U
-                        for (int j = 0; j < nk; ++j)
+                for (int j = 0; j < nk; ++j)
 #pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const T r = pd[0] * g[0][i] * w[1][j] * w[2][k] + pd[1] * w[0][i] * g[1][j] * w[2][k] +
-                                            pd[2] * w[0][i] * w[1][j] * g[2][k];
-                                atomic_add_array(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0, r);
-                            }
-                    break;
-                }
-                case CGX_TENSOR_DIVERGENCE_P2G:
-                case CGX_TENSOR_DIVERGENCE_T_P2G: {
-                    // pd[m][n]: the tensor entry paired with dW/dx_n for grid dof m
-                    const bool tr = op.kind == CGX_TENSOR_DIVERGENCE_T_P2G;
-                    T pd[3][3];
+                    for (int k = 0; k < nk; ++k) {
+                        const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+                        const T rg[3] = {g[0][i] * w[1][j] * w[2][k], w[0][i] * g[1][j] * w[2][k],
+                                         w[0][i] * w[1][j] * g[2][k]};
 #pragma unroll
-                    for (int a = 0; a < 3; ++a)
+                        for (int d0 = 0; d0 < 3; ++d0)
+                            atomic_add_array(op.a, n, d0,
+                                             rg[0] * pd[d0][0] + rg[1] * pd[d0][1] + rg[2] * pd[d0][2]);
+                    }
+            break;
+        }
+    }
+}
+
+// One G2P functor on point p (Interpolation.hpp:938-1182 over G2P::value /
+// gradient / divergence, :53-364): x += multiplier * result.
+template <int ORDER, class T>
+__device__ __forceinline__ void g2p_apply(const PointParams& prm, const DOp& op, int64_t p, const int* s,
+                                          const T (*w)[ORDER + 1], const T (*g)[ORDER + 1]) {
+    constexpr int nk = ORDER + 1;
+    constexpr int U = ORDER <= 3 ? nk : 1;
+    const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
+    switch (op.kind) {
+        case CGX_SCALAR_VALUE_G2P: {
+            T result = T(0);
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j)
+#pragma unroll U
+                    for (int k = 0; k < nk; ++k)
+                        result += load_array<T>(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0) *
+                                  w[0][i] * w[1][j] * w[2][k];
+            add_field<T>(op.x, p, 0, mult * result);
+            break;
+        }
+        case CGX_VECTOR_VALUE_G2P: {
+            T result[3] = {T(0), T(0), T(0)};
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j)
+#pragma unroll U
+                    for (int k = 0; k < nk; ++k) {
+                        const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+                        const T wijk = w[0][i] * w[1][j] * w[2][k];
 #pragma unroll
-                        for (int b = 0; b < 3; ++b) pd[a][b] = mult * load_field<T>(op.x, p, tr ? b * 3 + a : a * 3 + b);
-#pragma unroll U
-                    for (int i = 0; i < nk; ++i)
-#pragma unroll U
-                        for (int j = 0; j < nk; ++j)
-#pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
-                                const T rg[3] = {g[0][i] * w[1][j] * w[2][k], w[0][i] * g[1][j] * w[2][k],
-                                                 w[0][i] * w[1][j] * g[2][k]};
+                        for (int d = 0; d < 3; ++d) result[d] += load_array<T>(op.a, n, d) * wijk;
+                    }
 #pragma unroll
-                                for (int d0 = 0; d0 < 3; ++d0)
-                                    atomic_add_array(op.a, n, d0,
-                                                     rg[0] * pd[d0][0] + rg[1] * pd[d0][1] + rg[2] * pd[d0][2]);
-                            }
-                    break;
-                }
-            }
+            for (int d = 0; d < 3; ++d) add_field<T>(op.x, p, d, mult * result[d]);
+            break;
+        }
+        case CGX_SCALAR_GRADIENT_G2P: {
+            T result[3] = {T(0), T(0), T(0)};
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j)
+#pragma unroll U
+                    for (int k = 0; k < nk; ++k) {
+                        const T f = load_array<T>(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0);
+                        result[0] += f * g[0][i] * w[1][j] * w[2][k];
+                        result[1] += f * w[0][i] * g[1][j] * w[2][k];
+                        result[2] += f * w[0][i] * w[1][j] * g[2][k];
+                    }
+#pragma unroll
+            for (int d = 0; d < 3; ++d) add_field<T>(op.x, p, d, mult * result[d]);
+            break;
+        }
+        case CGX_VECTOR_GRADIENT_G2P:
+        case CGX_VECTOR_GRADIENT_T_G2P: {
+            // result[a][b] = sum dW/dx_a f_b, stored at (a, b) or transposed at (b, a)
+            const bool tr = op.kind == CGX_VECTOR_GRADIENT_T_G2P;
+            T result[3][3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) result[a][b] = T(0);
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j)
+#pragma unroll U
+                    for (int k = 0; k < nk; ++k) {
+                        const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+                        const T rg[3] = {g[0][i] * w[1][j] * w[2][k], w[0][i] * g[1][j] * w[2][k],
+                                         w[0][i] * w[1][j] * g[2][k]};
+                        T v[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) v[d] = load_array<T>(op.a, n, d);
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+#pragma unroll
+                            for (int b = 0; b < 3; ++b) result[a][b] += rg[a] * v[b];
+                    }
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) add_field<T>(op.x, p, tr ? b * 3 + a : a * 3 + b, mult * result[a][b]);
+            break;
+        }
+        case CGX_VECTOR_DIVERGENCE_G2P: {
+            T result = T(0);
+#pragma unroll U
+            for (int i = 0; i < nk; ++i)
+#pragma unroll U
+                for (int j = 0; j < nk; ++j)
+#pragma unroll U
+                    for (int k = 0; k < nk; ++k) {
+                        const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
+                        result += load_array<T>(op.a, n, 0) * g[0][i] * w[1][j] * w[2][k] +
+                                  load_array<T>(op.a, n, 1) * w[0][i] * g[1][j] * w[2][k] +
+                                  load_array<T>(op.a, n, 2) * w[0][i] * w[1][j] * g[2][k];
+                    }
+            add_field<T>(op.x, p, 0, result * mult);
+            break;
         }
     }
 }
 
 template <int ORDER, class T>
-__global__ void __launch_bounds__(256) g2p_points_kernel(const __grid_constant__ PointParams prm) {
-    using S = SplineKernel<ORDER, T>;
-    constexpr int nk = S::nk;
-    constexpr int U = ORDER <= 3 ? nk : 1;  // full unroll only for the hot orders
+__global__ void __launch_bounds__(256) p2g_points_kernel(const __grid_constant__ PointParams prm) {
+    constexpr int nk = ORDER + 1;
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < prm.num_point; p += stride) {
         int s[3];
         T w[3][nk], g[3][nk];
-        bool ok = true;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const double xp = load_field<double>(prm.points, p, d);
-            const double x0 = logical_coord<ORDER>(xp, prm.mesh.low[d], prm.mesh.rdx[d]);
-            T u;
-            base_and_offset<ORDER, T>(x0, s[d], u);
-            ok &= (x0 >= 0.0) && (s[d] >= 0) && (s[d] + nk <= prm.mesh.ext[d]);
-            if constexpr (sizeof(T) == 8)
-                S::weights(u, prm.mesh.rdx[d], w[d], g[d]);
-            else
-                S::weights(u, prm.mesh.rdx_f[d], w[d], g[d]);
-        }
-        if (!ok) {
+        if (!weights_3d<ORDER, T>(prm, p, s, w, g)) {
             raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
             continue;
         }
-        for (int o = 0; o < prm.n_ops; ++o) {
-            const DOp& op = prm.ops[o];
-            const T mult = sizeof(T) == 8 ? T(op.mult) : T(op.mult_f);
-            switch (op.kind) {
-                case CGX_SCALAR_VALUE_G2P: {
-                    T result = T(0);
-#pragma unroll U
-                    for (int i = 0; i < nk; ++i)
-#pragma unroll U
-                        for (int j = 0; j < nk; ++j)
-#pragma unroll U
-                            for (int k = 0; k < nk; ++k)
-                                result += load_array<T>(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0) *
-                                          w[0][i] * w[1][j] * w[2][k];
-                    add_field<T>(op.x, p, 0, mult * result);
-                    break;
-                }
-                case CGX_VECTOR_VALUE_G2P: {
-                    T result[3] = {T(0), T(0), T(0)};
-#pragma unroll U
-                    for (int i = 0; i < nk; ++i)
-#pragma unroll U
-                        for (int j = 0; j < nk; ++j)
-#pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
-                                const T wijk = w[0][i] * w[1][j] * w[2][k];
-#pragma unroll
-                                for (int d = 0; d < 3; ++d) result[d] += load_array<T>(op.a, n, d) * wijk;
-                            }
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) add_field<T>(op.x, p, d, mult * result[d]);
-                    break;
-                }
-                case CGX_SCALAR_GRADIENT_G2P: {
-                    T result[3] = {T(0), T(0), T(0)};
-#pragma unroll U
-                    for (int i = 0; i < nk; ++i)
-#pragma unroll U
-                        for (int j = 0; j < nk; ++j)
-#pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const T f = load_array<T>(op.a, node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k), 0);
-                                result[0] += f * g[0][i] * w[1][j] * w[2][k];
-                                result[1] += f * w[0][i] * g[1][j] * w[2][k];
-                                result[2] += f * w[0][i] * w[1][j] * g[2][k];
-                            }
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) add_field<T>(op.x, p, d, mult * result[d]);
-                    break;
-                }
-                case CGX_VECTOR_GRADIENT_G2P:
-                case CGX_VECTOR_GRADIENT_T_G2P: {
-                    // result[a][b] = sum dW/dx_a f_b, stored at (a, b) or transposed at (b, a)
-                    const bool tr = op.kind == CGX_VECTOR_GRADIENT_T_G2P;
-                    T result[3][3];
-#pragma unroll
-                    for (int a = 0; a < 3; ++a)
-#pragma unroll
-                        for (int b = 0; b < 3; ++b) result[a][b] = T(0);
-#pragma unroll U
-                    for (int i = 0; i < nk; ++i)
-#pragma unroll U
-                        for (int j = 0; j < nk; ++j)
-#pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
-                                const T rg[3] = {g[0][i] * w[1][j] * w[2][k], w[0][i] * g[1][j] * w[2][k],
-                                                 w[0][i] * w[1][j] * g[2][k]};
-                                T v[3];
-#pragma unroll
-                                for (int d = 0; d < 3; ++d) v[d] = load_array<T>(op.a, n, d);
-#pragma unroll
-                                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                                    for (int b = 0; b < 3; ++b) result[a][b] += rg[a] * v[b];
-                            }
-#pragma unroll
-                    for (int a = 0; a < 3; ++a)
-#pragma unroll
-                        for (int b = 0; b < 3; ++b) add_field<T>(op.x, p, tr ? b * 3 + a : a * 3 + b, mult * result[a][b]);
-                    break;
-                }
-                case CGX_VECTOR_DIVERGENCE_G2P: {
-                    T result = T(0);
-#pragma unroll U
-                    for (int i = 0; i < nk; ++i)
-#pragma unroll U
-                        for (int j = 0; j < nk; ++j)
-#pragma unroll U
-                            for (int k = 0; k < nk; ++k) {
-                                const int64_t n = node_index(prm.mesh, s[0] + i, s[1] + j, s[2] + k);
-                                result += load_array<T>(op.a, n, 0) * g[0][i] * w[1][j] * w[2][k] +
-                                          load_array<T>(op.a, n, 1) * w[0][i] * g[1][j] * w[2][k] +
-                                          load_array<T>(op.a, n, 2) * w[0][i] * w[1][j] * g[2][k];
-                            }
-                    add_field<T>(op.x, p, 0, result * mult);
-                    break;
-                }
-            }
+        for (int o = 0; o < prm.n_ops; ++o) p2g_apply<ORDER, T>(prm, prm.ops[o], p, s, w, g);
+    }
+}
+
+template <int ORDER, class T>
+__global__ void __launch_bounds__(256) g2p_points_kernel(const __grid_constant__ PointParams prm) {
+    constexpr int nk = ORDER + 1;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < prm.num_point; p += stride) {
+        int s[3];
+        T w[3][nk], g[3][nk];
+        if (!weights_3d<ORDER, T>(prm, p, s, w, g)) {
+            raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+            continue;
         }
+        for (int o = 0; o < prm.n_ops; ++o) g2p_apply<ORDER, T>(prm, prm.ops[o], p, s, w, g);
+    }
+}
+
+// Fused G2P then P2G per point (the g2p2g composition of
+// benchmark/grid/Cabana_Grid_InterpolationPerformance.cpp:129-174): one
+// spline evaluation, ops[0, n_g2p) gathered into their point fields, then
+// ops[n_g2p, n_ops) scattered from point fields that may hold the values just
+// gathered (same thread, program order).
+template <int ORDER, class T>
+__global__ void __launch_bounds__(256) g2p2g_points_kernel(const __grid_constant__ PointParams prm) {
+    constexpr int nk = ORDER + 1;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < prm.num_point; p += stride) {
+        int s[3];
+        T w[3][nk], g[3][nk];
+        if (!weights_3d<ORDER, T>(prm, p, s, w, g)) {
+            raise_error(prm.error_flag, CGX_ERR_OUT_OF_BOUNDS);
+            continue;
+        }
+        for (int o = 0; o < prm.n_g2p; ++o) g2p_apply<ORDER, T>(prm, prm.ops[o], p, s, w, g);
+        for (int o = prm.n_g2p; o < prm.n_ops; ++o) p2g_apply<ORDER, T>(prm, prm.ops[o], p, s, w, g);
     }
 }
 
@@ -527,6 +556,31 @@ cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64
         case 4: return launch_points_order<4>(prm, p2g, fp64, sms, st);
         case 5: return launch_points_order<5>(prm, p2g, fp64, sms, st);
         case 6: return launch_points_order<6>(prm, p2g, fp64, sms, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int ORDER>
+static cudaError_t launch_g2p2g_order(const PointParams& prm, bool fp64, int sms, cudaStream_t st) {
+    const int threads = 256;
+    const int blocks = grid_blocks(prm.num_point, threads, sms);
+    if (fp64)
+        g2p2g_points_kernel<ORDER, double><<<blocks, threads, 0, st>>>(prm);
+    else
+        g2p2g_points_kernel<ORDER, float><<<blocks, threads, 0, st>>>(prm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_g2p2g_points(const PointParams& prm, int order, bool fp64, int sms, cudaStream_t st) {
+    if (prm.num_point == 0) return cudaSuccess;
+    switch (order) {
+        case 0: return launch_g2p2g_order<0>(prm, fp64, sms, st);
+        case 1: return launch_g2p2g_order<1>(prm, fp64, sms, st);
+        case 2: return launch_g2p2g_order<2>(prm, fp64, sms, st);
+        case 3: return launch_g2p2g_order<3>(prm, fp64, sms, st);
+        case 4: return launch_g2p2g_order<4>(prm, fp64, sms, st);
+        case 5: return launch_g2p2g_order<5>(prm, fp64, sms, st);
+        case 6: return launch_g2p2g_order<6>(prm, fp64, sms, st);
     }
     return cudaErrorInvalidValue;
 }

@@ -314,6 +314,38 @@ def g2p(array, halo: Optional[Halo], points, num_point, spline: Spline, functor,
                             len(fs), precision, til, fl, _stream(stream)))
 
 
+def g2p2g(p2g_functor, points, num_point, spline: Spline, halo: Optional[Halo], p2g_array, g2p_functor,
+          g2p_array=None, *, precision=PLAIN_FP64, handle=None, stream=None, flags=0, check_bounds=False):
+    """Fused G2P then P2G per point, one spline evaluation (the g2p2g of
+    benchmark/grid/Cabana_Grid_InterpolationPerformance.cpp:129-174, whose
+    call shape `g2p2g(scalar_p2g, points, num_point, halo, array,
+    scalar_g2p)` this follows, plus the spline tag).
+
+    The G2P functors gather from `g2p_array` (default: `p2g_array`) into
+    their point fields; the P2G functors then scatter into `p2g_array`. G2P
+    reads each array as it was at the call (a snapshot where a P2G functor
+    also writes it). Lists of functors and arrays are accepted as in p2g /
+    g2p.
+    """
+    pf, pa = _as_list(p2g_functor), _as_list(p2g_array)
+    gf = _as_list(g2p_functor)
+    ga = _as_list(g2p_array) if g2p_array is not None else pa
+    if len(pa) == 1 and len(pf) > 1:
+        pa = pa * len(pf)
+    if len(ga) == 1 and len(gf) > 1:
+        ga = ga * len(gf)
+    if any(not f.p2g for f in pf) or any(f.p2g for f in gf):
+        raise TypeError("g2p2g needs P2G functors first and G2P functors last")
+    mesh = pa[0].mesh()
+    pops = _ops(pf, pa)
+    gops = _ops(gf, ga)
+    pts = field_descriptor(points)
+    h = handle or L.default_handle()
+    fl = flags | (0 if halo is not None else L.CGX_FLAG_SKIP_HALO) | (L.CGX_FLAG_CHECK_BOUNDS if check_bounds else 0)
+    L.check(L.lib().cgx_g2p2g(h.ptr, ctypes.byref(mesh), ctypes.byref(pts), int(num_point), spline.order, gops,
+                              len(gf), pops, len(pf), precision, fl, _stream(stream)))
+
+
 def createTensorDivergenceTransposedP2G(x, multiplier):
     """TensorDivergenceP2G of the transposed tensor (no reference
     counterpart): grid_m += sum_n dW/dx_n x[n][m]."""

@@ -207,6 +207,27 @@ cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points,
                    int n_ops, int precision, const cgx_tiling* tiling,
                    unsigned flags, void* stream);
 
+/*
+ * Fused grid-to-point-to-grid: the g2p2g composition of
+ * benchmark/grid/Cabana_Grid_InterpolationPerformance.cpp:129-174 (there a
+ * benchmark-local function; no library counterpart), generalised to several
+ * functors. Per point, one spline evaluation; the G2P functors add
+ * multiplier * result into their point fields, then the P2G functors
+ * scatter, reading point fields that may hold the values just gathered.
+ * G2P reads every array as it was at the call: an array that is also a P2G
+ * target is read from a snapshot taken first, so the result does not depend
+ * on the order in which points run (the reference benchmark reads and
+ * scatters into one array concurrently). Halo gather on the G2P arrays
+ * before, scatter(Sum) on the P2G arrays after, unless CGX_FLAG_SKIP_HALO.
+ * 3D meshes; point kernels in both precision forms; >= 1 functor of each
+ * direction, 8 in all.
+ */
+cgx_status cgx_g2p2g(cgx_handle h, const cgx_mesh* mesh,
+                     const cgx_field* points, int64_t num_point,
+                     int spline_order, const cgx_op* g2p_ops, int n_g2p,
+                     const cgx_op* p2g_ops, int n_p2g, int precision,
+                     unsigned flags, void* stream);
+
 /* ---- batched launches (no reference counterpart) ----------------------- */
 
 /*

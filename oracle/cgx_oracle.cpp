@@ -740,6 +740,51 @@ int oracle_g2p(const oracle_mesh* mesh, const double* points, int64_t num_point,
     return skipped;
 }
 
+// Fused g2p2g (the composition of benchmark/grid/
+// Cabana_Grid_InterpolationPerformance.cpp:129-174, with G2P reading every
+// array as it was at the call): halo.gather on the G2P arrays, then per
+// point one spline evaluation, the G2P functors, the P2G functors; then
+// halo.scatter(Sum) on the P2G arrays. 3D meshes only (returns -1 otherwise).
+int oracle_g2p2g(const oracle_mesh* mesh, const double* points, int64_t num_point, int order,
+                 const oracle_op* g2p_ops, int n_g2p, const oracle_op* p2g_ops, int n_p2g) {
+    if (dims(*mesh) != 3) return -1;
+    int64_t ext[3];
+    extents(*mesh, ext);
+    const int nd = 3;
+    for (int o = 0; o < n_g2p; ++o) {
+        bool seen = false;
+        for (int q = 0; q < o; ++q) seen |= (g2p_ops[q].array == g2p_ops[o].array);
+        if (!seen) oracle_halo_gather(mesh, g2p_ops[o].array, g2p_ops[o].dofs);
+    }
+    const int64_t nnode = ext[0] * ext[1] * ext[2];
+    std::vector<std::vector<double>> snaps(n_g2p);
+    std::vector<GridView> gviews, pviews;
+    for (int o = 0; o < n_g2p; ++o) {
+        double* src = g2p_ops[o].array;
+        snaps[o].assign(src, src + nnode * g2p_ops[o].dofs);  // the state at the call
+        gviews.push_back({snaps[o].data(), ext[0], ext[1], ext[2], g2p_ops[o].dofs});
+    }
+    for (int o = 0; o < n_p2g; ++o) pviews.push_back({p2g_ops[o].array, ext[0], ext[1], ext[2], p2g_ops[o].dofs});
+    int skipped = 0;
+    for (int64_t p = 0; p < num_point; ++p) {
+        Spline3 sd;
+        evaluate(*mesh, order, points + nd * p, sd);
+        if (!stencil_in_range(sd, ext, nd)) { ++skipped; continue; }
+        for (int o = 0; o < n_g2p; ++o)
+            g2p_point(g2p_ops[o].kind, g2p_ops[o].multiplier, g2p_ops[o].x + p * g2p_comps(g2p_ops[o].kind), sd,
+                      gviews[o]);
+        for (int o = 0; o < n_p2g; ++o)
+            p2g_point(p2g_ops[o].kind, p2g_ops[o].multiplier, p2g_ops[o].x + p * p2g_comps(p2g_ops[o].kind), sd,
+                      pviews[o]);
+    }
+    for (int o = 0; o < n_p2g; ++o) {
+        bool seen = false;
+        for (int q = 0; q < o; ++q) seen |= (p2g_ops[q].array == p2g_ops[o].array);
+        if (!seen) oracle_halo_scatter_sum(mesh, p2g_ops[o].array, p2g_ops[o].dofs);
+    }
+    return skipped;
+}
+
 // CartesianGrid::init, Cabana_CartesianGrid.hpp:61-73 and cellsBetween :279-283.
 void oracle_cartesian_num_bins(const double* grid_min, const double* grid_max,
                                const double* grid_delta, int32_t* nbin) {

@@ -79,6 +79,12 @@ int oracle_g2p(const oracle_mesh* mesh, const double* points,
                int64_t num_point, int order, const oracle_op* ops, int n_ops,
                int nthreads);
 
+// Fused g2p2g: per point the G2P functors (reading each array as it was at
+// the call) then the P2G functors; halo gather before, scatter after.
+int oracle_g2p2g(const oracle_mesh* mesh, const double* points,
+                 int64_t num_point, int order, const oracle_op* g2p_ops,
+                 int n_g2p, const oracle_op* p2g_ops, int n_p2g);
+
 void oracle_halo_scatter_sum(const oracle_mesh* mesh, double* array,
                              int dofs);
 void oracle_halo_gather(const oracle_mesh* mesh, double* array, int dofs);

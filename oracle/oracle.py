@@ -88,6 +88,8 @@ def lib():
         _lib.oracle_p2g.argtypes = [ctypes.POINTER(OracleMesh), dp, ctypes.c_int64, ctypes.c_int,
                                     ctypes.POINTER(OracleOp), ctypes.c_int, ctypes.c_int]
         _lib.oracle_g2p.argtypes = _lib.oracle_p2g.argtypes
+        _lib.oracle_g2p2g.argtypes = [ctypes.POINTER(OracleMesh), dp, ctypes.c_int64, ctypes.c_int,
+                                      ctypes.POINTER(OracleOp), ctypes.c_int, ctypes.POINTER(OracleOp), ctypes.c_int]
         _lib.oracle_spline_hessian.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, dp]
         _lib.oracle_p2g_adjoint.argtypes = [ctypes.POINTER(OracleMesh), dp, ctypes.c_int64, ctypes.c_int,
                                             ctypes.POINTER(OracleAdjointOp), ctypes.c_int, dp]
@@ -208,6 +210,17 @@ def g2p(mesh, points, order, ops, nthreads=1):
     n = points.shape[0]
     arr, _keep = _ops(ops, n, G2P_COMPS_2D if mesh.num_space_dim == 2 else G2P_COMPS)
     return lib().oracle_g2p(ctypes.byref(mesh), _dp(points), n, order, arr, len(ops), nthreads)
+
+
+def g2p2g(mesh, points, order, g2p_ops, p2g_ops):
+    """Fused g2p2g. g2p_ops / p2g_ops: lists of (kind, multiplier, x, array);
+    point fields and P2G arrays are updated in place; G2P reads each array as
+    it was at the call (its ghosts are gathered in place first)."""
+    points = np.ascontiguousarray(points, np.float64)
+    n = points.shape[0]
+    garr, _k1 = _ops(g2p_ops, n, G2P_COMPS)
+    parr, _k2 = _ops(p2g_ops, n, P2G_COMPS)
+    return lib().oracle_g2p2g(ctypes.byref(mesh), _dp(points), n, order, garr, len(g2p_ops), parr, len(p2g_ops))
 
 
 def _adjoint(fn, mesh, points, order, ops, points_bar):
