@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--batch-instances", type=int, default=512)
     ap.add_argument("--batch-seed", type=int, default=5)
     ap.add_argument("--no-precision", action="store_true", help="skip the large-origin precision sweep")
+    ap.add_argument("--no-g2p2g", action="store_true", help="skip the fused g2p2g leg")
     return ap.parse_args()
 
 
@@ -318,6 +319,62 @@ def batched_leg(args, dev):
                               "g2p_config": dict(zip(("item_particles", "ctas_per_sm"), gp.config())),
                               "autotune_s": tune_s},
             "speedup": per_ms / batch_ms}
+
+
+def g2p2g_leg(G, C, lg, pos, n, tiling, dev):
+    """The reference benchmark's scalar g2p2g (ScalarValueG2P(-0.5) then
+    ScalarValueP2G(-0.5) on one array, Spline<1>; benchmark/grid/
+    Cabana_Grid_InterpolationPerformance.cpp:129-174 and :454-510) on the
+    benchmark's particles: one fused launch against separate g2p + p2g calls
+    (point kernels, and the tiled kernels where the form allows)."""
+    import torch
+    out = {"workload": "scalar g2p2g, Spline<1>, one array read and written, benchmark particles (tile order)",
+           "particles": n}
+    for name, prec, dt in (("plain_fp64", G.PLAIN_FP64, torch.float64), ("fp32", G.FP32_COMPENSATED, torch.float32)):
+        arr = G.createArray("s", G.createArrayLayout(lg, 1, G.Node), dt)
+        scalar = torch.zeros(n, dtype=dt, device=dev)
+        halo = G.createHalo(G.NodeHaloPattern(), 1)
+        p2g_f, g2p_f = G.createScalarValueP2G(scalar, -0.5), G.createScalarValueG2P(scalar, -0.5)
+
+        def fused():
+            G.g2p2g(p2g_f, pos, n, G.Spline(1), halo, arr, g2p_f, precision=prec)
+
+        def separate(til):
+            G.g2p(arr, halo, pos, n, G.Spline(1), g2p_f, precision=prec, tiling=til)
+            G.p2g(p2g_f, pos, n, G.Spline(1), halo, arr, precision=prec, tiling=til)
+
+        def timed(fn, reps=3):
+            G.ArrayOp.assign(arr, 1.0, G.Ghost)
+            fn()
+            ts = []
+            for _ in range(reps):
+                G.ArrayOp.assign(arr, 1.0, G.Ghost)
+                scalar.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn()
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return sorted(ts)[len(ts) // 2]
+
+        r = {"fused_ms": timed(fused), "separate_points_ms": timed(lambda: separate(None))}
+        if prec == G.FP32_COMPENSATED:
+            # the tiled kernels need the Spline<1> tile order: a sorted copy
+            # of the positions (the field values are all zero, so only the
+            # coordinates move)
+            til1 = G.Tiling(tiling.mesh_params, 1, (8, 8, 8), device=dev)
+            pos1 = pos.clone()
+            C.permute_by(til1.sort(pos1, n), pos1)
+            r["separate_tiled_ms"] = timed(lambda: (
+                G.g2p(arr, halo, pos1, n, G.Spline(1), g2p_f, precision=prec, tiling=til1),
+                G.p2g(p2g_f, pos1, n, G.Spline(1), halo, arr, precision=prec, tiling=til1)))
+            del pos1, til1
+        r["fused_particles_per_s"] = n / (r["fused_ms"] / 1000.0)
+        out[name] = r
+        del arr, scalar
+    return out
 
 
 def precision_leg(args, dev):
@@ -698,6 +755,10 @@ def run_ours(args):
         batched = batched_leg(args, dev)
         torch.cuda.empty_cache()
     precision = None
+    fused = None
+    if rank == 0 and not args.no_g2p2g:
+        fused = g2p2g_leg(G, C, lg, pos, n, tiling, dev)
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_precision:
         precision = precision_leg(args, dev)
         torch.cuda.empty_cache()
@@ -725,7 +786,7 @@ def run_ours(args):
                                   "frac": step_bytes / (ms_per_step / 1000.0) / 1e9 / peak},
                 "kernels_ms": {"p2g": p2g_avg, "g2p": g2p_avg},
                 "cpu_baseline": cpu, "e2e": e2e, "plain_fp64": plain, "errors": errors,
-                "occupancy": occ, "binning_s": bin_s, "batched": batched, "large_origin_precision": precision, "gpu_launches": None, "clocks": clk}
+                "occupancy": occ, "binning_s": bin_s, "batched": batched, "g2p2g": fused, "large_origin_precision": precision, "gpu_launches": None, "clocks": clk}
         line["gpu_launches"] = launches_per_step() * args.steps
         print(json.dumps(line), flush=True)
     if world > 1:
