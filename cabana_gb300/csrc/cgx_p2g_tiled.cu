@@ -197,13 +197,13 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGe
     }
 }
 
-// Register accumulation of this lane's particle (zero coefficients for lanes
-// outside the current run). The coefficients are folded into the x-weights
-// first, so each (i, j) pair costs one product per channel (value) or three
-// (gradient) before the K fused multiply-adds per node.
+// Register accumulation of this lane's particle (lanes outside the current
+// run carry zero coefficients). The coefficients are folded into the
+// x-weights first, so each (i, j) pair costs one product per channel (value)
+// or three (gradient) before the K fused multiply-adds per node.
 template <int ORDER, int CH, bool GRAD>
 __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
-                                           const float (*coef)[3], bool member) {
+                                           const float (*coef)[3]) {
     constexpr int K = ORDER + 1;
     if (GRAD) {
         // node (i, j, k) += P_ij w_k + Q_ij g_k with
@@ -213,9 +213,9 @@ __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 
         for (int c = 0; c < CH; ++c)
 #pragma unroll
             for (int i = 0; i < K; ++i) {
-                a0[c][i] = member ? coef[c][0] * g[0][i] : 0.0f;
-                a1[c][i] = member ? coef[c][1] * w[0][i] : 0.0f;
-                a2[c][i] = member ? coef[c][2] * w[0][i] : 0.0f;
+                a0[c][i] = coef[c][0] * g[0][i];
+                a1[c][i] = coef[c][1] * w[0][i];
+                a2[c][i] = coef[c][2] * w[0][i];
             }
 #pragma unroll
         for (int i = 0; i < K; ++i)
@@ -241,7 +241,7 @@ __device__ __forceinline__ void accumulate(float* acc, const float (*w)[ORDER + 
 #pragma unroll
         for (int c = 0; c < CH; ++c)
 #pragma unroll
-            for (int i = 0; i < K; ++i) a0[c][i] = member ? coef[c][0] * w[0][i] : 0.0f;
+            for (int i = 0; i < K; ++i) a0[c][i] = coef[c][0] * w[0][i];
 #pragma unroll
         for (int i = 0; i < K; ++i)
 #pragma unroll
@@ -269,17 +269,16 @@ __device__ __forceinline__ void flush_run(float* acc, int lane, int key, const T
     constexpr int NODES = K * K * K;
     constexpr int R = NPAD / 32;
     transpose_reduce<NPAD>(acc, lane);
-    const int l2 = key % BB;
-    const int l1 = (key / BB) % BB;
-    const int l0 = key / (BB * BB);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int idx = lane * R + r;
         const int node = idx / CH;
         const int c = idx - node * CH;
         if (node < NODES && c < count && acc[r] != 0.0f) {
+            // stencil node (i, j, k) of base key (l0, l1, l2) sits at box index
+            // key + (i * BB + j) * BB + k
             const int i = node / (K * K), j = (node / K) % K, k = node % K;
-            const int bnode = ((l0 + i) * BB + (l1 + j)) * BB + (l2 + k);
+            const int bnode = key + (i * BB + j) * BB + k;
             const ChanSmem m = cs[first + c];
             const int e = m.sum_base + bnode * m.dofs;
             comp_add(box_smem + e, box_smem + e + m.comp_off, acc[r]);
@@ -360,7 +359,7 @@ __device__ __forceinline__ void run_piece(const TiledParams& prm, const TiledGeo
                 windows = 0;
             }
             ++windows;
-            accumulate<ORDER, CH, GRAD>(acc, w, g, coef, active);
+            accumulate<ORDER, CH, GRAD>(acc, w, g, coef);
         }
         flush_run<ORDER, TILE, CH, NPAD>(acc, lane, key, prm, box_smem, cs, first, count);
     }
