@@ -325,8 +325,9 @@ def g2p2g_leg(G, C, lg, pos, n, tiling, dev):
     """The reference benchmark's scalar g2p2g (ScalarValueG2P(-0.5) then
     ScalarValueP2G(-0.5) on one array, Spline<1>; benchmark/grid/
     Cabana_Grid_InterpolationPerformance.cpp:129-174 and :454-510) on the
-    benchmark's particles: one fused launch against separate g2p + p2g calls
-    (point kernels, and the tiled kernels where the form allows)."""
+    benchmark's particles: the fused point kernel against separate g2p + p2g
+    calls (point kernels, and the tiled kernels where the form allows), and
+    cgx_g2p2g given a tiling (the tiled pair)."""
     import torch
     out = {"workload": "scalar g2p2g, Spline<1>, one array read and written, benchmark particles (tile order)",
            "particles": n}
@@ -337,7 +338,7 @@ def g2p2g_leg(G, C, lg, pos, n, tiling, dev):
         p2g_f, g2p_f = G.createScalarValueP2G(scalar, -0.5), G.createScalarValueG2P(scalar, -0.5)
 
         def fused():
-            G.g2p2g(p2g_f, pos, n, G.Spline(1), halo, arr, g2p_f, precision=prec)
+            G.g2p2g(p2g_f, pos, n, G.Spline(1), halo, arr, g2p_f, precision=prec)  # fused point kernel
 
         def separate(til):
             G.g2p(arr, halo, pos, n, G.Spline(1), g2p_f, precision=prec, tiling=til)
@@ -370,6 +371,9 @@ def g2p2g_leg(G, C, lg, pos, n, tiling, dev):
             r["separate_tiled_ms"] = timed(lambda: (
                 G.g2p(arr, halo, pos1, n, G.Spline(1), g2p_f, precision=prec, tiling=til1),
                 G.p2g(p2g_f, pos1, n, G.Spline(1), halo, arr, precision=prec, tiling=til1)))
+            # cgx_g2p2g given the tiling runs the tiled pair itself
+            r["g2p2g_tiled_ms"] = timed(lambda: G.g2p2g(p2g_f, pos1, n, G.Spline(1), halo, arr, g2p_f,
+                                                         precision=prec, tiling=til1))
             del pos1, til1
         r["fused_particles_per_s"] = n / (r["fused_ms"] / 1000.0)
         out[name] = r

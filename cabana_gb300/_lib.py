@@ -153,7 +153,7 @@ def lib():
     L.cgx_p2g.argtypes = interp
     L.cgx_g2p.argtypes = interp
     L.cgx_g2p2g.argtypes = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, ctypes.c_int, P(CgxOp), ctypes.c_int, P(CgxOp),
-                            ctypes.c_int, ctypes.c_int, ctypes.c_uint, vp]
+                            ctypes.c_int, ctypes.c_int, P(CgxTiling), ctypes.c_uint, vp]
     adj = [vp, P(CgxMesh), P(CgxField), ctypes.c_int64, ctypes.c_int, P(CgxAdjointOp), ctypes.c_int, ctypes.c_int,
            P(CgxTiling), P(CgxField), ctypes.c_uint, vp]
     L.cgx_p2g_adjoint.argtypes = adj

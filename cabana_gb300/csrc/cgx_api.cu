@@ -774,8 +774,8 @@ cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, 
 }
 
 cgx_status cgx_g2p2g(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, int64_t num_point, int spline_order,
-                     const cgx_op* g2p_ops, int n_g2p, const cgx_op* p2g_ops, int n_p2g, int precision, unsigned flags,
-                     void* stream) {
+                     const cgx_op* g2p_ops, int n_g2p, const cgx_op* p2g_ops, int n_p2g, int precision,
+                     const cgx_tiling* tiling, unsigned flags, void* stream) {
     if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
     cgx_status s = check_mesh(mesh);
     if (s) return s;
@@ -795,6 +795,18 @@ cgx_status cgx_g2p2g(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points
     if (s) return s;
     s = check_ops(p2g_ops, n_p2g, true, num_point > 0);
     if (s) return s;
+    if (tiling && precision == CGX_FP32_COMPENSATED && num_point > 0) {
+        // G2P completes over all points before P2G writes: the same contract
+        // as the fused kernel, with the tiled kernels where they apply
+        s = interpolate(h, mesh, points, num_point, spline_order, g2p_ops, n_g2p, precision, tiling, flags, stream,
+                        false);
+        if (s) return s;
+        const int g2p_dispatch = h->last_dispatch;
+        s = interpolate(h, mesh, points, num_point, spline_order, p2g_ops, n_p2g, precision, tiling, flags, stream,
+                        true);
+        if (!s && g2p_dispatch != CGX_DISPATCH_TILED) h->last_dispatch = g2p_dispatch;
+        return s;
+    }
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (flags & CGX_FLAG_CHECK_BOUNDS) CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
     if (!(flags & CGX_FLAG_SKIP_HALO)) {

@@ -315,7 +315,8 @@ def g2p(array, halo: Optional[Halo], points, num_point, spline: Spline, functor,
 
 
 def g2p2g(p2g_functor, points, num_point, spline: Spline, halo: Optional[Halo], p2g_array, g2p_functor,
-          g2p_array=None, *, precision=PLAIN_FP64, handle=None, stream=None, flags=0, check_bounds=False):
+          g2p_array=None, *, precision=PLAIN_FP64, tiling=None, handle=None, stream=None, flags=0,
+          check_bounds=False):
     """Fused G2P then P2G per point, one spline evaluation (the g2p2g of
     benchmark/grid/Cabana_Grid_InterpolationPerformance.cpp:129-174, whose
     call shape `g2p2g(scalar_p2g, points, num_point, halo, array,
@@ -325,7 +326,8 @@ def g2p2g(p2g_functor, points, num_point, spline: Spline, halo: Optional[Halo], 
     their point fields; the P2G functors then scatter into `p2g_array`. G2P
     reads each array as it was at the call (a snapshot where a P2G functor
     also writes it). Lists of functors and arrays are accepted as in p2g /
-    g2p.
+    g2p. With a `tiling` and the FP32 form the tiled G2P then P2G launches
+    run (same results, faster); otherwise one fused point kernel.
     """
     pf, pa = _as_list(p2g_functor), _as_list(p2g_array)
     gf = _as_list(g2p_functor)
@@ -342,8 +344,9 @@ def g2p2g(p2g_functor, points, num_point, spline: Spline, halo: Optional[Halo], 
     pts = field_descriptor(points)
     h = handle or L.default_handle()
     fl = flags | (0 if halo is not None else L.CGX_FLAG_SKIP_HALO) | (L.CGX_FLAG_CHECK_BOUNDS if check_bounds else 0)
+    til = ctypes.byref(tiling.struct) if tiling is not None else None
     L.check(L.lib().cgx_g2p2g(h.ptr, ctypes.byref(mesh), ctypes.byref(pts), int(num_point), spline.order, gops,
-                              len(gf), pops, len(pf), precision, fl, _stream(stream)))
+                              len(gf), pops, len(pf), precision, til, fl, _stream(stream)))
 
 
 def createTensorDivergenceTransposedP2G(x, multiplier):

@@ -219,14 +219,17 @@ cgx_status cgx_g2p(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points,
  * on the order in which points run (the reference benchmark reads and
  * scatters into one array concurrently). Halo gather on the G2P arrays
  * before, scatter(Sum) on the P2G arrays after, unless CGX_FLAG_SKIP_HALO.
- * 3D meshes; point kernels in both precision forms; >= 1 functor of each
- * direction, 8 in all.
+ * 3D meshes; >= 1 functor of each direction, 8 in all. Without a tiling
+ * (or in the plain FP64 form) one fused point kernel runs; with a tiling
+ * that the tiled kernels take (as for cgx_p2g) the tiled G2P launch then
+ * the tiled P2G launch run, which gives the same results faster because
+ * their shared-memory node boxes avoid per-point global atomics.
  */
 cgx_status cgx_g2p2g(cgx_handle h, const cgx_mesh* mesh,
                      const cgx_field* points, int64_t num_point,
                      int spline_order, const cgx_op* g2p_ops, int n_g2p,
                      const cgx_op* p2g_ops, int n_p2g, int precision,
-                     unsigned flags, void* stream);
+                     const cgx_tiling* tiling, unsigned flags, void* stream);
 
 /* ---- batched launches (no reference counterpart) ----------------------- */
 

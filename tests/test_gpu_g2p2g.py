@@ -96,3 +96,49 @@ def test_mpm_style_g2p2g_vs_oracle(oracle, form_name, precision, order):
         assert max_rel(got.double().cpu().numpy(), ref) <= tol, (form_name, order)
     # the read array is left as it was (no functor writes it)
     assert max_rel(a_mom.view().double().cpu().numpy(), r_momsrc) <= (1e-15 if precision == G.PLAIN_FP64 else 1e-7)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_tiled_g2p2g_vs_oracle(oracle, order):
+    """With a tiling and the FP32 form, cgx_g2p2g runs the tiled G2P then the
+    tiled P2G launch: the same contract (G2P reads the state at the call)."""
+    from cabana_gb300 import core
+    lg, mp = M.simple_mesh((10, 9, 8), 0.5, (0.3, -1.1, 2.0), 2)
+    om = oracle_mesh(oracle, mp)
+    rng = np.random.default_rng(1200 + order)
+    n = 20000
+    lo = np.array(mp.ghost_low) + 2 * 0.5
+    pts = lo + rng.uniform(0.0, 1.0, size=(n, 3)) * (np.array((10, 9, 8)) * 0.5)
+    ext = mp.extents()
+    mom = rng.normal(size=ext + (3,))
+    sgrid = rng.normal(size=ext + (1,))
+    vel0 = rng.normal(size=(n, 3))
+    s0 = rng.normal(size=(n, 1))
+    mass = rng.uniform(0.5, 1.5, size=(n, 1))
+    r_vel, r_s, r_mass, r_mom2, r_sg, r_mom = (vel0.copy(), s0.copy(), np.zeros(ext + (1,)), np.zeros(ext + (3,)),
+                                               sgrid.copy(), mom.copy())
+    assert oracle.g2p2g(om, pts, order, [(1, 1.0, r_vel, r_mom), (0, -0.5, r_s, r_sg)],
+                        [(0, 1.0, mass, r_mass), (1, 0.7, r_vel, r_mom2), (0, -0.5, r_s, r_sg)]) == 0
+    tp = torch.tensor(pts, device="cuda")
+    vel = torch.tensor(vel0, device="cuda").float()
+    s = torch.tensor(s0[:, 0], device="cuda").float()
+    tmass = torch.tensor(mass[:, 0], device="cuda").float()
+    til = G.Tiling(mp, order, (8, 8, 8))
+    perm = til.sort(tp, n)
+    core.permute_by(perm, tp, vel, s, tmass)
+    perm = perm.cpu().numpy()
+    lay = lambda d: G.createArrayLayout(lg, d, M.Node)  # noqa: E731
+    a_mom = G.createArray("mom", lay(3), torch.float32)
+    a_mom.view().copy_(torch.tensor(mom, device="cuda").float())
+    a_s = G.createArray("s", lay(1), torch.float32)
+    a_s.view().copy_(torch.tensor(sgrid, device="cuda").float())
+    a_mass, a_mom2 = G.createArray("m", lay(1), torch.float32), G.createArray("p", lay(3), torch.float32)
+    G.g2p2g([G.createScalarValueP2G(tmass, 1.0), G.createVectorValueP2G(vel, 0.7), G.createScalarValueP2G(s, -0.5)],
+            tp, n, G.Spline(order), G.createHalo(G.NodeHaloPattern(), 2), [a_mass, a_mom2, a_s],
+            [G.createVectorValueG2P(vel, 1.0), G.createScalarValueG2P(s, -0.5)], [a_mom, a_s],
+            precision=G.FP32_COMPENSATED, tiling=til, check_bounds=True)
+    assert G.last_dispatch() == "tiled"
+    assert max_rel(vel.double().cpu().numpy(), r_vel[perm]) <= 4e-6
+    assert max_rel(s.double().cpu().numpy(), r_s[perm, 0]) <= 4e-6
+    for got, ref in [(a_mass, r_mass), (a_mom2, r_mom2), (a_s, r_sg)]:
+        assert max_rel(got.view().double().cpu().numpy(), ref) <= 2e-6, order
