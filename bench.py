@@ -730,7 +730,9 @@ def run_ours(args):
 
         for k in range(max(nsets, args.warmup)):
             e2e_step(k)
-        esteps = max(6, min(args.steps, 9))
+        # a streaming run: enough steps that filling and draining the
+        # pipeline (one step's compute and read-back, ~70 ms) is amortised
+        esteps = min(32, max(16, 2 * args.steps))
         torch.cuda.synchronize()
         barrier()
         s0 = torch.cuda.Event(enable_timing=True)
