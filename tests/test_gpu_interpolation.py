@@ -366,3 +366,78 @@ def test_empty_point_set():
     G.p2g(G.createScalarValueP2G(x, 1.0), pts, 0, G.Spline(2), None, arr)
     G.g2p(arr, None, pts, 0, G.Spline(2), G.createScalarValueG2P(x, 1.0))
     assert arr.view().abs().sum().item() == 0.0
+
+
+@pytest.mark.parametrize("layout_name", ["layout_left", "aosoa"])
+def test_tiled_fp32_with_strided_and_aosoa_fields(oracle, layout_name):
+    """The tiled FP32 kernels on point fields that are not dense rows: a
+    LayoutLeft View (components n apart) or AoSoA slices (VL = 32), staged
+    component by component. Mass + momentum + stress divergence, then
+    velocity + velocity gradient."""
+    lg, mp = small_mesh()
+    rng = np.random.default_rng(77)
+    n = 6000
+    lo, hi = domain(mp)
+    pts = clumped_points(rng, n, lo, hi, 4, 0.6)
+    m = rng.uniform(0.5, 1.5, size=(n, 1))
+    mom = m * rng.normal(size=(n, 3))
+    sig = rng.normal(size=(n, 9))
+    om = oracle_mesh(oracle, mp)
+    mass_ref = np.zeros(mp.extents() + (1,))
+    mom_ref = np.zeros(mp.extents() + (3,))
+    frc_ref = np.zeros(mp.extents() + (3,))
+    oracle.p2g(om, pts, 2, [(0, 1.0, m, mass_ref), (1, 1.0, mom, mom_ref), (4, -1.0, sig, frc_ref)])
+    vel_ref = np.zeros((n, 3))
+    vg_ref = np.zeros((n, 9))
+    oracle.g2p(om, pts, 2, [(1, 1.0, vel_ref, mom_ref.copy()), (3, 1.0, vg_ref, mom_ref.copy())])
+    # tile order, applied on the host so every layout holds sorted data
+    til = G.Tiling(mp, 2, (8, 8, 8))
+    perm = til.sort(torch.tensor(pts, device="cuda"), n).cpu().numpy()
+    pts_s, m_s, mom_s, sig_s = pts[perm], m[perm], mom[perm], sig[perm]
+    tp = torch.tensor(pts_s, device="cuda")
+    f32 = torch.float32
+    if layout_name == "layout_left":
+        tm = torch.tensor(m_s[:, 0], device="cuda").to(f32)
+        tmom = torch.tensor(mom_s.T.copy(), device="cuda").to(f32).t()                     # (n, 3), strides (1, n)
+        tsig = torch.tensor(sig_s.reshape(n, 3, 3).transpose(1, 2, 0).copy(), device="cuda").to(f32).permute(2, 0, 1)
+        vel = torch.zeros((3, n), dtype=f32, device="cuda").t()
+        vg = torch.zeros((3, 3, n), dtype=f32, device="cuda").permute(2, 0, 1)
+        read_vel = lambda: vel.double().cpu().numpy()  # noqa: E731
+        read_vg = lambda: vg.double().cpu().numpy().reshape(n, 9)  # noqa: E731
+    else:
+        vl = 32
+        nsoa = (n + vl - 1) // vl
+        pad = nsoa * vl - n
+
+        def soa(a):  # (n, c) -> (nsoa, c, vl)
+            return np.concatenate([a, np.zeros((pad, a.shape[1]))]).reshape(nsoa, vl, a.shape[1]).transpose(0, 2, 1)
+
+        # AoSoA<float mass, float[3] mom, float[3][3] stress>: 13 floats x VL per SoA
+        storage = torch.tensor(np.concatenate([soa(m_s), soa(mom_s), soa(sig_s)], axis=1).reshape(-1), device="cuda").to(f32)
+        tm = G.Slice(storage, 0, vl, 13 * vl, 1, n)
+        tmom = G.Slice(storage, vl, vl, 13 * vl, 3, n)
+        tsig = G.Slice(storage, 4 * vl, vl, 13 * vl, 9, n)
+        # AoSoA<float[3] vel, float[3][3] velgrad>: 12 floats x VL per SoA
+        out = torch.zeros(nsoa * 12 * vl, dtype=f32, device="cuda")
+        vel = G.Slice(out, 0, vl, 12 * vl, 3, n)
+        vg = G.Slice(out, 3 * vl, vl, 12 * vl, 9, n)
+
+        def unsoa(first, c):
+            a = out.double().cpu().numpy().reshape(nsoa, 12, vl)[:, first:first + c, :]
+            return a.transpose(0, 2, 1).reshape(nsoa * vl, c)[:n]
+
+        read_vel = lambda: unsoa(0, 3)  # noqa: E731
+        read_vg = lambda: unsoa(3, 9)  # noqa: E731
+    mass = G.createArray("mass", layout(lg, 1), f32)
+    momg = G.createArray("mom", layout(lg, 3), f32)
+    frc = G.createArray("frc", layout(lg, 3), f32)
+    G.p2g([G.createScalarValueP2G(tm, 1.0), G.createVectorValueP2G(tmom, 1.0), G.createTensorDivergenceP2G(tsig, -1.0)],
+          tp, n, G.Spline(2), None, [mass, momg, frc], precision=G.FP32_COMPENSATED, tiling=til, check_bounds=True)
+    assert G.last_dispatch() == "tiled"
+    for got, ref in [(mass, mass_ref), (momg, mom_ref), (frc, frc_ref)]:
+        assert max_rel(got.view().double().cpu().numpy(), ref) <= TOL_P2G_FP32, layout_name
+    G.g2p(momg, None, tp, n, G.Spline(2), [G.createVectorValueG2P(vel, 1.0), G.createVectorGradientG2P(vg, 1.0)],
+          precision=G.FP32_COMPENSATED, tiling=til, check_bounds=True)
+    assert G.last_dispatch() == "tiled"
+    assert max_rel(read_vel(), vel_ref[perm]) <= 4 * TOL_G2P_FP32, layout_name
+    assert max_rel(read_vg(), vg_ref[perm]) <= 4 * TOL_G2P_FP32, layout_name
