@@ -79,12 +79,6 @@ __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) 
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
 }
 
-// Asynchronous 16-byte global -> shared copy (both addresses 16-byte aligned).
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
-}
-
 // ---- bulk copies (TMA) tracked by a shared-memory mbarrier -----------------
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -176,12 +170,6 @@ __device__ __forceinline__ void prefetch_field_range(const DField& f, int64_t b,
     const uintptr_t lo = reinterpret_cast<uintptr_t>(f.data + b * f.soa_stride * elt) & ~uintptr_t(15);
     const uintptr_t hi = (reinterpret_cast<uintptr_t>(f.data + e * f.soa_stride * elt) + 15) & ~uintptr_t(15);
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"(unsigned(hi - lo)) : "memory");
-}
-
-// Ask the L1 to fetch the line holding element (p, c) of a field.
-__device__ __forceinline__ void prefetch_field(const DField& f, int64_t p, int c) {
-    const int64_t o = field_offset(f, p, c) * (f.dtype == CGX_F64 ? 8 : 4);
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(f.data + o));
 }
 
 template <class T>
@@ -376,43 +364,6 @@ __device__ __forceinline__ void base_and_offset(double x0, int& base, T& u) {
     const int c = static_cast<int>(x0);
     base = c + first_offset(ORDER);
     u = T(x0 - double(c));
-}
-
-// Integer part and in-cell offset of a non-negative logical coordinate t
-// held in a double, using integer operations only (the double pipe runs at
-// 1/64 of the FP32 rate on this part). The offset is truncated to 32
-// fraction bits, then to FP32 toward zero, so it is always < 1. Returns
-// false for t < 0, t >= 2^30 or NaN.
-__device__ __forceinline__ bool split_logical(double t, int& cell, float& u) {
-    // Range checks on the bits (no double-precision compares): negative,
-    // >= 2^30, infinite and NaN values all fail.
-    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(t));
-    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-    const int e = int(mag >> 52);
-    if (mag == 0 || e == 0) {  // +-0 or subnormal
-        cell = 0;
-        u = 0.0f;
-        return true;
-    }
-    if ((b >> 63) != 0 || e >= 1023 + 30) {
-        cell = 0;
-        u = 0.0f;
-        return false;
-    }
-    const unsigned long long sig = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1075 - e;  // t = sig * 2^-sh
-    unsigned int ufx;
-    if (sh > 52) {  // t < 1
-        cell = 0;
-        const int r = sh - 32;
-        ufx = r >= 53 ? 0u : static_cast<unsigned int>(sig >> r);
-    } else {
-        cell = int(sig >> sh);
-        const unsigned long long fr = sig & ((1ull << sh) - 1ull);
-        ufx = sh >= 32 ? static_cast<unsigned int>(fr >> (sh - 32)) : static_cast<unsigned int>(fr << (32 - sh));
-    }
-    u = __uint2float_rz(ufx) * 2.3283064365386963e-10f;  // * 2^-32
-    return true;
 }
 
 // The mapping t = x * rdx + c0 of one dimension in integer form, for the
