@@ -157,7 +157,7 @@ __device__ __forceinline__ float pick(const float* v, int idx) {
 template <int ORDER, int TILE, int CH, bool GRAD>
 __device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGeom& geo, float* box_smem, const ChanSmem* cs, int first,
                                            int count, const float (*w)[ORDER + 1], const float (*g)[ORDER + 1],
-                                           const float (*coef)[3], bool inbox, const int* l, const int* s, int lane) {
+                                           const float (*coef)[3], bool inbox, int key, const int* s, int lane) {
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
     constexpr int NODES = K * K * K;
@@ -175,7 +175,7 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGe
         } else {
             wv = wi * wj * wk;
         }
-        const int bnode = inbox ? ((l[0] + i) * BB + (l[1] + j)) * BB + (l[2] + k) : 0;
+        const int bnode = inbox ? key + (i * BB + j) * BB + k : 0;  // box node of stencil node (i, j, k)
         const int64_t gnode = inbox ? 0 : node_index(geo.mesh, s[0] + i, s[1] + j, s[2] + k);
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
@@ -371,10 +371,9 @@ __device__ __forceinline__ void run_piece(const TiledParams& prm, const TiledGeo
 template <int ORDER, int TILE, bool GRAD>
 __device__ __forceinline__ void run_window(const TiledParams& prm, const TiledGeom& geo, float* box_smem,
                                            const float4* prep, const float* srcs, const int* src_off,
-                                           const int* src_str, int i, const ChanSmem* cs, int gi, const int* origin,
+                                           const int* src_str, int i, const ChanSmem* cs, int gi,
                                            int64_t item_begin, int lane) {
     using SH = P2GShape<ORDER>;
-    constexpr int BB = TILE + ORDER;
     constexpr int K = SH::K;
     constexpr int CH = GRAD ? SH::CG : SH::CV;
     const GroupCoef<CH, GRAD ? 3 : 1> gc(prm, gi, src_off, src_str);
@@ -390,19 +389,13 @@ __device__ __forceinline__ void run_window(const TiledParams& prm, const TiledGe
         float w[3][K], g[3][K];
 #pragma unroll
         for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], geo.mesh.rdx_f[d], w[d], g[d]);
-        int l[3], s[3];
+        int s[3] = {0, 0, 0};  // global base node, for a stencil outside the box
         const bool inbox = key >= 0;
-        if (inbox) {
-            l[2] = key % BB;
-            l[1] = (key / BB) % BB;
-            l[0] = key / (BB * BB);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) s[d] = origin[d] + l[d];
-        } else {
+        if (!inbox) {
             float uu[3];
             form_point<ORDER>(geo, item_begin + i, s, uu);
         }
-        add_direct<ORDER, TILE, CH, GRAD>(prm, geo, box_smem, cs, first, count, w, g, coef, inbox, l, s, lane);
+        add_direct<ORDER, TILE, CH, GRAD>(prm, geo, box_smem, cs, first, count, w, g, coef, inbox, key, s, lane);
     }
 }
 
@@ -755,10 +748,10 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                     const int k = wi * 32 + lane;
                     const int i = k < ndir ? int(dlist[k]) : -1;  // item particle of this lane, or none
                     if (prm.groups[gi].gradient)
-                        run_window<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, src_off, src_str, i, cs, gi, origin, cb,
+                        run_window<ORDER, TILE, true>(prm, geo, box_smem, prep, srcs, src_off, src_str, i, cs, gi, cb,
                                                       lane);
                     else
-                        run_window<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, src_off, src_str, i, cs, gi, origin, cb,
+                        run_window<ORDER, TILE, false>(prm, geo, box_smem, prep, srcs, src_off, src_str, i, cs, gi, cb,
                                                       lane);
                 }
             }

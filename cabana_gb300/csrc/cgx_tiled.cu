@@ -73,9 +73,12 @@ __device__ __forceinline__ bool form_point(const TiledGeom& geo, int64_t p, int*
 }
 
 // Gather sums for one array: V[n] = sum W v_n, D[m][n] = sum d_m W v_n.
+// BOXED: the stencil's base node is box node `key`, and stencil node
+// (i, j, k) is box node key + (i * BB + j) * BB + k; otherwise the array is
+// read at the global nodes s + (i, j, k).
 template <int ORDER, int TILE, int NDOF, bool GRAD, bool BOXED>
-__device__ __forceinline__ void gather_sums(const TiledGeom& geo, const DArray& arr, const float* box,
-                                            const int* l, const int* s, const float (*w)[ORDER + 1],
+__device__ __forceinline__ void gather_sums(const TiledGeom& geo, const DArray& arr, const float* box, int key,
+                                            const int* s, const float (*w)[ORDER + 1],
                                             const float (*g)[ORDER + 1], float* V, float (*D)[3]) {
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
@@ -101,7 +104,7 @@ __device__ __forceinline__ void gather_sums(const TiledGeom& geo, const DArray& 
                 float v[NDOF];
                 if (BOXED) {
                     // box nodes are padded to 4 floats for 3 dofs: one 16-byte load per node
-                    const int node = ((l[0] + i) * BB + (l[1] + j)) * BB + (l[2] + k);
+                    const int node = key + (i * BB + j) * BB + k;
                     if constexpr (NDOF == 3) {
                         const float4 q = reinterpret_cast<const float4*>(box)[node];
                         v[0] = q.x;
@@ -409,16 +412,13 @@ __global__ void __launch_bounds__(kThreads, 2)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) SplineKernel<ORDER, float>::weights(u[d], geo.mesh.rdx_f[d], w[d], g[d]);
                 float V[NDOF], D[3][3];
-                int l[3], s[3];
+                int s[3];
                 if (key >= 0) {
-                    l[2] = key % BB;
-                    l[1] = (key / BB) % BB;
-                    l[0] = key / (BB * BB);
-                    gather_sums<ORDER, TILE, NDOF, GRAD, true>(geo, arr, box, l, s, w, g, V, D);
+                    gather_sums<ORDER, TILE, NDOF, GRAD, true>(geo, arr, box, key, s, w, g, V, D);
                 } else {
                     float uu[3];
                     form_point<ORDER>(geo, sb + i, s, uu);
-                    gather_sums<ORDER, TILE, NDOF, GRAD, false>(geo, arr, box, l, s, w, g, V, D);
+                    gather_sums<ORDER, TILE, NDOF, GRAD, false>(geo, arr, box, 0, s, w, g, V, D);
                 }
                 apply_ops<NDOF>(prm, om, out, i, V, D);
             }
