@@ -412,7 +412,6 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     __shared__ int item_idx;
     __shared__ int runs[kChunk + 1];
     __shared__ int2 pieces[kMaxPieces];
-    __shared__ unsigned char run_direct[kChunk];  // per run: its particles are added directly
     __shared__ int16_t dlist[kChunk];             // particles added directly, in order
     __shared__ int n_runs, n_big, n_direct;
     __shared__ int next_run[2 * kMaxGroups];
@@ -596,7 +595,6 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             // particles.
             constexpr int PER = kChunk / kThreads;
             int keys[PER];
-            int rid[PER];  // run index of each of this thread's particles
             {
                 double xs[PER][3];
 #pragma unroll
@@ -642,20 +640,32 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int i = threadIdx.x * PER + q;
                 keys[q] = i < len ? __float_as_int(prep[i].w) : kKeyInvalid;
             }
-            // Run starts: particle i starts a run when its key differs from i-1.
+            // Runs of equal keys and the particles added directly, from one
+            // block scan: particle i starts a run when its key differs from
+            // i-1, and is added directly when its stencil leaves the box (key
+            // -1) or it is alone in its run (its key differs from both
+            // neighbours); runs of two or more inside the box become pieces.
+            // The direct list keeps item order so its windows are full.
+            static_assert(kSmallRun == 2, "the direct test compares a particle with its two neighbours");
             {
-                int flags = 0, nstart = 0;
+                int flags = 0, dflags = 0, nstart = 0, nd = 0;
 #pragma unroll
                 for (int q = 0; q < PER; ++q) {
                     const int i = threadIdx.x * PER + q;
-                    int prev = kKeyInvalid - 1;
+                    const int key = keys[q];
+                    int prev = kKeyInvalid - 1, next = kKeyInvalid - 1;
                     if (i > 0) prev = q == 0 ? __float_as_int(prep[i - 1].w) : keys[q - 1];
-                    const bool st = i < len && keys[q] != prev;
+                    if (i + 1 < len) next = q == PER - 1 ? __float_as_int(prep[i + 1].w) : keys[q + 1];
+                    const bool st = i < len && key != prev;
+                    const bool d = i < len && key != kKeyInvalid && (key < 0 || (key != prev && key != next));
                     flags |= st ? (1 << q) : 0;
                     nstart += st ? 1 : 0;
+                    dflags |= d ? (1 << q) : 0;
+                    nd += d ? 1 : 0;
                 }
-                // block exclusive scan of nstart
-                int x = nstart;
+                // block exclusive scan of (nstart, nd), packed in one int (each < 2^16)
+                const int mine = nstart | (nd << 16);
+                int x = mine;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -663,62 +673,32 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 }
                 if (lane == 31) warp_sums[warp] = x;
                 __syncthreads();
-                int wp = 0;
-                for (int w2 = 0; w2 < warp; ++w2) wp += warp_sums[w2];
-                int pos = wp + x - nstart;
+                int ex = x - mine;
+                for (int w2 = 0; w2 < warp; ++w2) ex += warp_sums[w2];
+                int pos = ex & 0xFFFF, dpos = ex >> 16;
 #pragma unroll
                 for (int q = 0; q < PER; ++q) {
                     if (flags & (1 << q)) runs[pos++] = threadIdx.x * PER + q;
-                    rid[q] = pos - 1;  // run of particle threadIdx.x * PER + q
+                    if (dflags & (1 << q)) dlist[dpos++] = int16_t(threadIdx.x * PER + q);
                 }
                 if (threadIdx.x == kThreads - 1) {
                     n_runs = pos;
                     runs[pos] = len;
+                    n_direct = dpos;
                 }
             }
             __syncthreads();
-            // Classify runs: long runs inside the box go to the big list, the
-            // particles of the others are added directly, window by window.
+            // Long runs inside the box are cut into pieces.
             for (int r = threadIdx.x; r < n_runs; r += blockDim.x) {
                 const int rb = runs[r], re = runs[r + 1];
                 const int key = __float_as_int(prep[rb].w);
-                const bool is_big = key >= 0 && re - rb >= kSmallRun;
-                if (is_big) {
+                if (key >= 0 && re - rb >= kSmallRun) {
                     // n_big counts pieces: at most kChunk / kPiece + (number of big runs) <= kMaxPieces
                     const int np = (re - rb + kPiece - 1) / kPiece;
                     const int base = atomicAdd(&n_big, np);
                     for (int q = 0; q < np; ++q)
                         pieces[base + q] = make_int2(rb + q * kPiece, min(re, rb + (q + 1) * kPiece));
                 }
-                run_direct[r] = (!is_big && key != kKeyInvalid) ? 1 : 0;
-            }
-            __syncthreads();
-            // The particles added directly, compacted into a list (in order)
-            // so their windows are full: each thread flags its own particles
-            // and a block scan places them.
-            {
-                int dflags = 0, nd = 0;
-#pragma unroll
-                for (int q = 0; q < PER; ++q) {
-                    const int i = threadIdx.x * PER + q;
-                    const bool d = i < len && run_direct[rid[q]] != 0;
-                    dflags |= d ? (1 << q) : 0;
-                    nd += d ? 1 : 0;
-                }
-                int x = nd;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int y = __shfl_up_sync(0xffffffffu, x, o);
-                    if (lane >= o) x += y;
-                }
-                if (lane == 31) warp_sums[warp] = x;
-                __syncthreads();
-                int pos = x - nd;
-                for (int w2 = 0; w2 < warp; ++w2) pos += warp_sums[w2];
-#pragma unroll
-                for (int q = 0; q < PER; ++q)
-                    if (dflags & (1 << q)) dlist[pos++] = int16_t(threadIdx.x * PER + q);
-                if (threadIdx.x == kThreads - 1) n_direct = pos;
             }
             __syncthreads();
             {
