@@ -128,6 +128,35 @@ cudaError_t launch_order(const AdjointParams& prm, bool fp64, int sms, cudaStrea
 
 }  // namespace
 
+// Position adjoint of a value term from its gradient sums: grads holds, per
+// point, D[e][c] = sum_n A_c(n) dW_n/dx_e at grads[p * 3 * ncomp + e * ncomp
+// + c] (a ScalarGradientG2P / VectorGradientG2P of A with multiplier 1), so
+// dL/dx_e += mult * sum_c s_c D[e][c].
+__global__ void __launch_bounds__(256) adjoint_value_combine_kernel(DField points_bar, DField sf, const float* grads,
+                                                                    int64_t n, int ncomp, float mult) {
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride) {
+        float sv[3] = {0.0f, 0.0f, 0.0f};
+        for (int c = 0; c < ncomp; ++c) sv[c] = load_field<float>(sf, p, c);
+        const float* D = grads + p * 3 * ncomp;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            float r = 0.0f;
+            for (int c = 0; c < ncomp; ++c) r = fmaf(sv[c], D[e * ncomp + c], r);
+            add_field<double>(points_bar, p, e, double(mult * r));
+        }
+    }
+}
+
+cudaError_t launch_adjoint_value_combine(const DField& points_bar, const DField& sf, const float* grads, int64_t n,
+                                         int ncomp, float mult, int sms, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    int64_t b = (n + 255) / 256;
+    if (b > int64_t(sms) * 16) b = int64_t(sms) * 16;
+    adjoint_value_combine_kernel<<<int(b), 256, 0, st>>>(points_bar, sf, grads, n, ncomp, mult);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_adjoint_points(const AdjointParams& prm, int order, bool fp64, int sms, cudaStream_t st) {
     if (prm.num_point == 0 || prm.n_terms == 0) return cudaSuccess;
     switch (order) {

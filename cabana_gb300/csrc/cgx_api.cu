@@ -19,6 +19,8 @@ struct cgx_context {
     size_t work_cap = 0;
     int64_t* work_prefix = nullptr;
     size_t prefix_cap = 0;
+    void* adj = nullptr;  // grow-only: gradient sums of the position adjoint
+    size_t adj_bytes = 0;
     int last_dispatch = CGX_DISPATCH_NONE;
 };
 
@@ -672,7 +674,48 @@ cgx_status adjoint(cgx_handle h, const cgx_mesh* mesh, const cgx_field* points, 
             if (!seen) CGX_CUDA(launch_halo(to_halo(*mesh, ops[o].array_bar), kHaloGatherAdd, h->sms, st));
         }
     }
-    if (want_pos && num_point > 0) {
+    // Value terms (ScalarValue / VectorValue pairings) in the FP32 form with
+    // a tiling: dL/dx is the point field against the gradient sums of the
+    // array, which the tiled G2P forms (ScalarGradientG2P / VectorGradientG2P
+    // into a scratch field), then one combine kernel; other terms take the
+    // point kernel.
+    bool value_only = want_pos && num_point > 0 && precision == CGX_FP32_COMPENSATED && tiling &&
+                      spline_order >= 1 && spline_order <= 3;
+    for (int o = 0; o < n_ops && value_only; ++o) {
+        const int pat = adjoint_pattern(ops[o].kind, p2g);
+        value_only = pat == kAdjValue1 || pat == kAdjValue3;
+    }
+    if (value_only) {
+        const size_t need = size_t(num_point) * 9 * sizeof(float);
+        if (need > h->adj_bytes) {
+            if (h->adj) cudaFree(h->adj);
+            h->adj = nullptr;
+            h->adj_bytes = 0;
+            if (cudaMalloc(&h->adj, need) != cudaSuccess) return fail(CGX_ERR_NO_MEMORY, "adjoint scratch allocation failed");
+            h->adj_bytes = need;
+        }
+        float* grads = reinterpret_cast<float*>(h->adj);
+        for (int o = 0; o < n_ops; ++o) {
+            const bool vec = adjoint_pattern(ops[o].kind, p2g) == kAdjValue3;
+            const int nc = vec ? 3 : 1;
+            CGX_CUDA(cudaMemsetAsync(grads, 0, size_t(num_point) * 3 * nc * sizeof(float), st));
+            cgx_op g;
+            std::memset(&g, 0, sizeof(g));
+            g.kind = vec ? CGX_VECTOR_GRADIENT_G2P : CGX_SCALAR_GRADIENT_G2P;
+            g.multiplier = 1.0;
+            g.x.data = grads;
+            g.x.dtype = CGX_F32;
+            g.x.vector_length = 1;
+            g.x.soa_stride = 3 * nc;
+            g.x.comp_stride = 1;
+            g.array = p2g ? ops[o].array_bar : ops[o].array;
+            s = interpolate(h, mesh, points, num_point, spline_order, &g, 1, precision, tiling, inner, stream, false);
+            if (s) return s;
+            const cgx_field& sf = p2g ? ops[o].x : ops[o].x_bar;
+            CGX_CUDA(launch_adjoint_value_combine(to_dfield(*points_bar), to_dfield(sf), grads, num_point, nc,
+                                                  float(ops[o].multiplier), h->sms, st));
+        }
+    } else if (want_pos && num_point > 0) {
         AdjointParams prm;
         std::memset(&prm, 0, sizeof(prm));
         prm.mesh = to_dmesh(*mesh);
@@ -745,6 +788,7 @@ cgx_status cgx_destroy(cgx_handle h) {
     if (h->flags) cudaFree(h->flags);
     if (h->work) cudaFree(h->work);
     if (h->work_prefix) cudaFree(h->work_prefix);
+    if (h->adj) cudaFree(h->adj);
     delete h;
     return CGX_OK;
 }

@@ -171,6 +171,10 @@ cudaError_t launch_points(const PointParams& prm, int order, bool p2g, bool fp64
 // Fused g2p2g on the point kernels (3D): ops[0, prm.n_g2p) G2P, then P2G.
 cudaError_t launch_g2p2g_points(const PointParams& prm, int order, bool fp64, int sms, cudaStream_t st);
 cudaError_t launch_adjoint_points(const AdjointParams& prm, int order, bool fp64, int sms, cudaStream_t st);
+// dL/dx_e += mult * sum_c s_c D[e][c] from the gradient sums D of a value
+// term (grads: per point 3 x ncomp floats, ncomp 1 or 3).
+cudaError_t launch_adjoint_value_combine(const DField& points_bar, const DField& sf, const float* grads, int64_t n,
+                                         int ncomp, float mult, int sms, cudaStream_t st);
 cudaError_t launch_halo(const HaloParams& h, int mode, int sms, cudaStream_t st);
 cudaError_t launch_fill(void* data, int dtype, int64_t count, double value, int sms, cudaStream_t st);
 
