@@ -18,14 +18,15 @@
 //    spline) so a lane holds its group's whole stencil (27 nodes x channels)
 //    in registers. The CTA's 16 warps pull units of work -- (piece, group)
 //    and then (window, group) -- from shared counters.
-//  * Runs of two or more particles are cut into pieces of <= 1024 particles
+//  * Runs of eight or more particles (two or more for the cubic spline) are
+//    cut into pieces of <= 1024 particles
 //    (a dense cell keeps every warp busy). A piece is walked 32 particles at
 //    a time, one particle per lane, each lane adding its particle into its registers; at the end of
 //    the piece the warp reduces the registers across lanes with a
 //    transpose-reduction (each lane ends with 1/32 of the sums) and adds them
 //    into the box with compensated shared atomics -- one shared atomic per
 //    node and channel per piece instead of one per particle.
-//  * Single particles of their cell (and stencils outside the box) are
+//  * The particles of shorter runs (and stencils outside the box) are
 //    compacted into a list, taken 32 at a time and added directly, each lane
 //    walking its stencil from a different node so lanes do not collide;
 //    outside the box they go to global memory with bounds checks, so the tile
@@ -46,11 +47,21 @@ constexpr int kChunk = 2048;        // particles staged in shared memory at a ti
 // tiles flush once per kItem particles.
 constexpr int kItem = 16384;
 constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows per lane
-constexpr int kSmallRun = 2;        // shorter runs (single particles) add each particle directly
+// Runs shorter than small_run<ORDER>() add each particle directly: a warp
+// reduction costs about as much as adding a few particles one by one, and a
+// short run leaves most of a window's lanes idle. A direct particle costs one
+// shared atomic per stencil node and channel, so the threshold falls with the
+// stencil size: 8 for linear and quadratic (measured best on clumped and
+// uniform quadratic workloads against 2, 16 and 32), 2 (single particles)
+// for cubic, where 64-node direct adds made a uniform 2^24-particle P2G 27 %
+// slower at 8.
+constexpr int kMinSmallRun = 2;
+template <int ORDER>
+__host__ __device__ constexpr int small_run() { return ORDER >= 3 ? 2 : 8; }
 // Long runs are cut into pieces of at most kPiece particles so that all the
 // warps of a channel group share a dense cell, each piece reduced on its own.
 constexpr int kPiece = 1024;
-constexpr int kMaxPieces = kChunk / kSmallRun + kChunk / kPiece + 1;
+constexpr int kMaxPieces = kChunk / kMinSmallRun + kChunk / kPiece + 1;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
 constexpr int kKeyInvalid = -2;     // stencil outside the ghosted index space
 
@@ -412,6 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
     __shared__ int item_idx;
     __shared__ int runs[kChunk + 1];
     __shared__ int2 pieces[kMaxPieces];
+    __shared__ unsigned char run_direct[kChunk];  // per run: its particles are added directly
     __shared__ int16_t dlist[kChunk];             // particles added directly, in order
     __shared__ int n_runs, n_big, n_direct;
     __shared__ int next_run[2 * kMaxGroups];
@@ -595,6 +607,7 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
             // particles.
             constexpr int PER = kChunk / kThreads;
             int keys[PER];
+            int rid[PER];  // run index of each of this thread's particles
             {
                 double xs[PER][3];
 #pragma unroll
@@ -640,32 +653,20 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const int i = threadIdx.x * PER + q;
                 keys[q] = i < len ? __float_as_int(prep[i].w) : kKeyInvalid;
             }
-            // Runs of equal keys and the particles added directly, from one
-            // block scan: particle i starts a run when its key differs from
-            // i-1, and is added directly when its stencil leaves the box (key
-            // -1) or it is alone in its run (its key differs from both
-            // neighbours); runs of two or more inside the box become pieces.
-            // The direct list keeps item order so its windows are full.
-            static_assert(kSmallRun == 2, "the direct test compares a particle with its two neighbours");
+            // Run starts: particle i starts a run when its key differs from i-1.
             {
-                int flags = 0, dflags = 0, nstart = 0, nd = 0;
+                int flags = 0, nstart = 0;
 #pragma unroll
                 for (int q = 0; q < PER; ++q) {
                     const int i = threadIdx.x * PER + q;
-                    const int key = keys[q];
-                    int prev = kKeyInvalid - 1, next = kKeyInvalid - 1;
+                    int prev = kKeyInvalid - 1;
                     if (i > 0) prev = q == 0 ? __float_as_int(prep[i - 1].w) : keys[q - 1];
-                    if (i + 1 < len) next = q == PER - 1 ? __float_as_int(prep[i + 1].w) : keys[q + 1];
-                    const bool st = i < len && key != prev;
-                    const bool d = i < len && key != kKeyInvalid && (key < 0 || (key != prev && key != next));
+                    const bool st = i < len && keys[q] != prev;
                     flags |= st ? (1 << q) : 0;
                     nstart += st ? 1 : 0;
-                    dflags |= d ? (1 << q) : 0;
-                    nd += d ? 1 : 0;
                 }
-                // block exclusive scan of (nstart, nd), packed in one int (each < 2^16)
-                const int mine = nstart | (nd << 16);
-                int x = mine;
+                // block exclusive scan of nstart
+                int x = nstart;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -673,32 +674,62 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 }
                 if (lane == 31) warp_sums[warp] = x;
                 __syncthreads();
-                int ex = x - mine;
-                for (int w2 = 0; w2 < warp; ++w2) ex += warp_sums[w2];
-                int pos = ex & 0xFFFF, dpos = ex >> 16;
+                int wp = 0;
+                for (int w2 = 0; w2 < warp; ++w2) wp += warp_sums[w2];
+                int pos = wp + x - nstart;
 #pragma unroll
                 for (int q = 0; q < PER; ++q) {
                     if (flags & (1 << q)) runs[pos++] = threadIdx.x * PER + q;
-                    if (dflags & (1 << q)) dlist[dpos++] = int16_t(threadIdx.x * PER + q);
+                    rid[q] = pos - 1;  // run of particle threadIdx.x * PER + q
                 }
                 if (threadIdx.x == kThreads - 1) {
                     n_runs = pos;
                     runs[pos] = len;
-                    n_direct = dpos;
                 }
             }
             __syncthreads();
-            // Long runs inside the box are cut into pieces.
+            // Classify runs: long runs inside the box go to the big list, the
+            // particles of the others are added directly, window by window.
             for (int r = threadIdx.x; r < n_runs; r += blockDim.x) {
                 const int rb = runs[r], re = runs[r + 1];
                 const int key = __float_as_int(prep[rb].w);
-                if (key >= 0 && re - rb >= kSmallRun) {
+                const bool is_big = key >= 0 && re - rb >= small_run<ORDER>();
+                if (is_big) {
                     // n_big counts pieces: at most kChunk / kPiece + (number of big runs) <= kMaxPieces
                     const int np = (re - rb + kPiece - 1) / kPiece;
                     const int base = atomicAdd(&n_big, np);
                     for (int q = 0; q < np; ++q)
                         pieces[base + q] = make_int2(rb + q * kPiece, min(re, rb + (q + 1) * kPiece));
                 }
+                run_direct[r] = (!is_big && key != kKeyInvalid) ? 1 : 0;
+            }
+            __syncthreads();
+            // The particles added directly, compacted into a list (in order)
+            // so their windows are full: each thread flags its own particles
+            // and a block scan places them.
+            {
+                int dflags = 0, nd = 0;
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const int i = threadIdx.x * PER + q;
+                    const bool d = i < len && run_direct[rid[q]] != 0;
+                    dflags |= d ? (1 << q) : 0;
+                    nd += d ? 1 : 0;
+                }
+                int x = nd;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) warp_sums[warp] = x;
+                __syncthreads();
+                int pos = x - nd;
+                for (int w2 = 0; w2 < warp; ++w2) pos += warp_sums[w2];
+#pragma unroll
+                for (int q = 0; q < PER; ++q)
+                    if (dflags & (1 << q)) dlist[pos++] = int16_t(threadIdx.x * PER + q);
+                if (threadIdx.x == kThreads - 1) n_direct = pos;
             }
             __syncthreads();
             {
