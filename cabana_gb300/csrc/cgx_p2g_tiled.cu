@@ -172,6 +172,15 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGe
     constexpr int BB = TILE + ORDER;  // node box extent per dimension
     constexpr int K = ORDER + 1;
     constexpr int NODES = K * K * K;
+    // Box offsets of the channels, read once: shared-memory atomics in the
+    // loop would otherwise make the compiler reload them at every node.
+    int cbase[CH], cdofs[CH];
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+        const ChanSmem m = cs[first + (c < count ? c : 0)];
+        cbase[c] = m.sum_base + m.comp_off;  // node 0 of the compensation half
+        cdofs[c] = m.dofs;
+    }
     int node = lane % NODES;
 #pragma unroll 1
     for (int step = 0; step < NODES; ++step) {
@@ -193,12 +202,10 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGe
             if (c >= count) break;
             const float v = GRAD ? coef[c][0] * g0 + coef[c][1] * g1 + coef[c][2] * g2 : coef[c][0] * wv;
             if (inbox) {
-                // Single-particle terms go to the compensation half with a
-                // plain (non-returning) atomic: they are small next to the
-                // run sums held in the sum half, and the flush adds both.
-                const ChanSmem m = cs[first + c];
-                const int e = m.sum_base + bnode * m.dofs;
-                atomicAdd(box_smem + e + m.comp_off, v);
+                // Direct terms go to the compensation half with a plain
+                // (non-returning) atomic: they are small next to the run
+                // sums held in the sum half, and the flush adds both.
+                atomicAdd(box_smem + cbase[c] + bnode * cdofs[c], v);
             } else {
                 const Channel& ch = prm.channels[first + c];
                 atomic_add_array(geo.arr[ch.slot], gnode, ch.dof, v);
