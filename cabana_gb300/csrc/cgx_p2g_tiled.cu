@@ -181,6 +181,49 @@ __device__ __forceinline__ void add_direct(const TiledParams& prm, const TiledGe
         cbase[c] = m.sum_base + m.comp_off;  // node 0 of the compensation half
         cdofs[c] = m.dofs;
     }
+    if (inbox) {
+        // Inside the box: the lane starts at layer i = lane % K and walks the
+        // K layers cyclically, each layer's K x K (j, k) nodes in a fixed
+        // order, with the (j, k) weight products formed once. Lanes of one
+        // short run (consecutive lanes, same base node) then start on
+        // different layers.
+        float ajk[K][K], bjk[K][K], cjk[K][K];
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                ajk[j][k] = w[1][j] * w[2][k];
+                bjk[j][k] = GRAD ? g[1][j] * w[2][k] : 0.0f;
+                cjk[j][k] = GRAD ? w[1][j] * g[2][k] : 0.0f;
+            }
+        int i = lane % K;
+#pragma unroll 1
+        for (int layer = 0; layer < K; ++layer) {
+            const float wi = pick<K>(w[0], i);
+            const float gi = GRAD ? pick<K>(g[0], i) : 0.0f;
+            const int lbase = key + i * (BB * BB);  // box node of stencil node (i, 0, 0)
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const int bnode = lbase + j * BB + k;
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        if (c >= count) break;
+                        const float v = GRAD ? coef[c][0] * (gi * ajk[j][k]) + coef[c][1] * (wi * bjk[j][k]) +
+                                                   coef[c][2] * (wi * cjk[j][k])
+                                             : coef[c][0] * (wi * ajk[j][k]);
+                        // Direct terms go to the compensation half with a
+                        // plain (non-returning) atomic: they are small next to
+                        // the run sums held in the sum half, and the flush
+                        // adds both.
+                        atomicAdd(box_smem + cbase[c] + bnode * cdofs[c], v);
+                    }
+                }
+            i = (i + 1 == K) ? 0 : i + 1;
+        }
+        return;
+    }
     int node = lane % NODES;
 #pragma unroll 1
     for (int step = 0; step < NODES; ++step) {
