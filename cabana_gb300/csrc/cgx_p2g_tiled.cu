@@ -58,8 +58,9 @@ constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows pe
 constexpr int kMinSmallRun = 2;
 template <int ORDER>
 __host__ __device__ constexpr int small_run() { return ORDER >= 3 ? 2 : 8; }
-// Long runs are cut into pieces of at most kPiece particles so that all the
-// warps of a channel group share a dense cell, each piece reduced on its own.
+// Long runs are cut into pieces of equal length, at most kPiece particles, so
+// that all the warps of a channel group share a dense cell, each piece reduced
+// on its own.
 constexpr int kPiece = 1024;
 constexpr int kMaxPieces = kChunk / kMinSmallRun + kChunk / kPiece + 1;
 constexpr int kKeyOutside = -1;     // stencil inside the mesh but outside the box
@@ -72,6 +73,8 @@ struct P2GShape {
     // Channels per group, sized so a lane's stencil sums fit in <= 128
     // registers (16 warps per SM).
     static constexpr int CV = ORDER >= 3 ? 1 : (ORDER == 2 ? 2 : 4);  // value channels per group
+    // Two gradient channels per quadratic group also fit without spills but
+    // made the clumped 2^27-particle P2G 10 % slower (10.59 ms against 9.66).
     static constexpr int CG = ORDER >= 2 ? 1 : 3;                     // gradient channels per group
     static constexpr int pad32(int v) { return (v + 31) / 32 * 32; }
     static constexpr int NV = pad32(NODES * CV);
@@ -746,10 +749,13 @@ __global__ void __launch_bounds__(kThreads, 1) p2g_tiled_kernel(const __grid_con
                 const bool is_big = key >= 0 && re - rb >= small_run<ORDER>();
                 if (is_big) {
                     // n_big counts pieces: at most kChunk / kPiece + (number of big runs) <= kMaxPieces
-                    const int np = (re - rb + kPiece - 1) / kPiece;
+                    // np pieces of equal length (to within one particle), so
+                    // no short remainder piece leaves its warp idle early
+                    const int len_r = re - rb;
+                    const int np = (len_r + kPiece - 1) / kPiece;
                     const int base = atomicAdd(&n_big, np);
                     for (int q = 0; q < np; ++q)
-                        pieces[base + q] = make_int2(rb + q * kPiece, min(re, rb + (q + 1) * kPiece));
+                        pieces[base + q] = make_int2(rb + q * len_r / np, rb + (q + 1) * len_r / np);
                 }
                 run_direct[r] = (!is_big && key != kKeyInvalid) ? 1 : 0;
             }
