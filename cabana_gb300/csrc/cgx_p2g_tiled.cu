@@ -18,7 +18,7 @@
 //    spline) so a lane holds its group's whole stencil (27 nodes x channels)
 //    in registers. The CTA's 16 warps pull units of work -- (piece, group)
 //    and then (window, group) -- from shared counters.
-//  * Runs of eight or more particles (two or more for the cubic spline) are
+//  * Runs of six or more particles (two or more for the cubic spline) are
 //    cut into pieces of <= 1024 particles
 //    (a dense cell keeps every warp busy). A piece is walked 32 particles at
 //    a time, one particle per lane, each lane adding its particle into its registers; at the end of
@@ -51,13 +51,13 @@ constexpr int kMaxRunWindows = 32;  // register sums cover at most 32 windows pe
 // reduction costs about as much as adding a few particles one by one, and a
 // short run leaves most of a window's lanes idle. A direct particle costs one
 // shared atomic per stencil node and channel, so the threshold falls with the
-// stencil size: 8 for linear and quadratic (measured best on clumped and
-// uniform quadratic workloads against 2, 16 and 32), 2 (single particles)
-// for cubic, where 64-node direct adds made a uniform 2^24-particle P2G 27 %
-// slower at 8.
+// stencil size: 6 for linear and quadratic, 2 (single particles) for cubic,
+// where 64-node direct adds made a uniform 2^24-particle P2G 27 % slower at 8.
+// Quadratic, clumped 2^27 particles / 2^24 uniform + clump, P2G (+ G2P) ms:
+// threshold 4: 9.50 / 7.43, 6: 9.54 / 7.04, 8: 9.62 / 7.26, 12: 9.99 / 9.44.
 constexpr int kMinSmallRun = 2;
 template <int ORDER>
-__host__ __device__ constexpr int small_run() { return ORDER >= 3 ? 2 : 8; }
+__host__ __device__ constexpr int small_run() { return ORDER >= 3 ? 2 : 6; }
 // Long runs are cut into pieces of equal length, at most kPiece particles, so
 // that all the warps of a channel group share a dense cell, each piece reduced
 // on its own.
