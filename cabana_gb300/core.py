@@ -45,40 +45,69 @@ class BinningData:
 
 
 class LinkedCellList:
+    """LinkedCellList<MemorySpace, double, NumSpaceDim> (core/src/Cabana_LinkedCellList.hpp),
+    NumSpaceDim = len(grid_min): 3 (positions (p, 0..2)) or 2 (positions (p, 0..1))."""
+
     def __init__(self, positions, grid_delta, grid_min, grid_max, begin=0, end=None, handle=None, stream=None):
+        nd = len(grid_min)
+        if nd not in (2, 3) or len(grid_max) != nd or len(grid_delta) != nd:
+            raise ValueError("grid_min / grid_max / grid_delta need 2 or 3 entries each")
         n = positions.size if isinstance(positions, Slice) else positions.shape[0]
         end = n if end is None else end
         d3 = ctypes.c_double * 3
         nb = (ctypes.c_int32 * 3)()
-        self._min, self._max, self._delta = d3(*grid_min), d3(*grid_max), d3(*grid_delta)
+        # bin counts: a 2D grid is counted as a 3D one with a single z cell
+        pad = lambda v, fill: d3(*(list(v) + [fill] * (3 - nd)))  # noqa: E731
+        self._min, self._max, self._delta = pad(grid_min, 0.0), pad(grid_max, 1.0), pad(grid_delta, 1.0)
         L.check(L.lib().cgx_cartesian_num_bins(self._min, self._max, self._delta, nb))
-        self._nbin = tuple(nb)
-        total = self._nbin[0] * self._nbin[1] * self._nbin[2]
+        self._nbin = tuple(nb)[:nd]
+        total = self.totalBins()
         dev = positions.storage.device if isinstance(positions, Slice) else positions.device
         counts = torch.zeros(total, dtype=torch.int32, device=dev)
         offsets = torch.zeros(total, dtype=torch.int64, device=dev)
         permutes = torch.zeros(max(1, end - begin), dtype=torch.int64, device=dev)
         h = handle or L.default_handle()
-        L.check(L.lib().cgx_linked_cell_build(h.ptr, ctypes.byref(field_descriptor(positions)), begin, end,
-                                              self._min, self._max, self._delta,
-                                              ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(offsets.data_ptr()),
-                                              ctypes.c_void_p(permutes.data_ptr()), _stream(stream)))
+        outs = (ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(offsets.data_ptr()),
+                ctypes.c_void_p(permutes.data_ptr()), _stream(stream))
+        desc = ctypes.byref(field_descriptor(positions))
+        if nd == 3:
+            L.check(L.lib().cgx_linked_cell_build(h.ptr, desc, begin, end, self._min, self._max, self._delta, *outs))
+        else:
+            d2 = ctypes.c_double * 2
+            L.check(L.lib().cgx_linked_cell_build_2d(h.ptr, desc, begin, end, d2(*grid_min), d2(*grid_max),
+                                                     d2(*grid_delta), *outs))
         self._data = BinningData(begin, end, counts, offsets, permutes[: end - begin])
 
     def numBin(self, d):
         return self._nbin[d]
 
     def totalBins(self):
-        return self._nbin[0] * self._nbin[1] * self._nbin[2]
+        t = 1
+        for b in self._nbin:
+            t *= b
+        return t
 
-    def cardinalBinIndex(self, i, j, k):
-        return (i * self._nbin[1] + j) * self._nbin[2] + k
+    def _ijk(self, ijk):
+        # binSize(i, j[, k]) or binSize((i, j[, k])) -- the reference's
+        # Kokkos::Array overload
+        if len(ijk) == 1 and isinstance(ijk[0], (tuple, list)):
+            ijk = tuple(ijk[0])
+        if len(ijk) != len(self._nbin):
+            raise ValueError(f"need {len(self._nbin)} cell indices")
+        return ijk
 
-    def binSize(self, i, j, k):
-        return self._data.binSize(self.cardinalBinIndex(i, j, k))
+    def cardinalBinIndex(self, *ijk):
+        ijk = self._ijk(ijk)
+        c = 0
+        for d, x in enumerate(ijk):
+            c = c * self._nbin[d] + x
+        return c
 
-    def binOffset(self, i, j, k):
-        return self._data.binOffset(self.cardinalBinIndex(i, j, k))
+    def binSize(self, *ijk):
+        return self._data.binSize(self.cardinalBinIndex(*ijk))
+
+    def binOffset(self, *ijk):
+        return self._data.binOffset(self.cardinalBinIndex(*ijk))
 
     def permutation(self, i):
         return self._data.permutation(i)

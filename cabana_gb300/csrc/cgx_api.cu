@@ -988,9 +988,15 @@ cgx_status cgx_cartesian_num_bins(const double grid_min[3], const double grid_ma
     return CGX_OK;
 }
 
-cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions, int64_t begin, int64_t end,
-                                 const double grid_min[3], const double grid_max[3], const double grid_delta[3],
-                                 int32_t* counts, uint64_t* offsets, uint64_t* permutes, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// LinkedCellList::build for `dims` (2 or 3) coordinates; grid arrays have
+// `dims` entries.
+cgx_status linked_cell_build(cgx_handle h, const cgx_field* positions, int dims, int64_t begin, int64_t end,
+                             const double* grid_min, const double* grid_max, const double* grid_delta,
+                             int32_t* counts, uint64_t* offsets, uint64_t* permutes, void* stream) {
     if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
     cgx_status s = check_field(positions, "positions");
     if (s) return s;
@@ -998,15 +1004,23 @@ cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions, int64
     if (begin < 0 || end < begin) return fail(CGX_ERR_INVALID_ARG, "need 0 <= begin <= end");
     if (end - begin >= (int64_t(1) << 32)) return fail(CGX_ERR_NOT_SUPPORTED, "more than 2^32 - 1 particles");
     if (!counts || !offsets || (!permutes && end > begin)) return fail(CGX_ERR_INVALID_ARG, "NULL output");
+    if (!grid_min || !grid_max || !grid_delta) return fail(CGX_ERR_INVALID_ARG, "NULL argument");
+    // Pad a 2D grid with one z cell of width 1 (never read by the key kernel).
+    double gmin[3] = {0.0, 0.0, 0.0}, gmax[3] = {1.0, 1.0, 1.0}, gdel[3] = {1.0, 1.0, 1.0};
+    for (int d = 0; d < dims; ++d) {
+        gmin[d] = grid_min[d];
+        gmax[d] = grid_max[d];
+        gdel[d] = grid_delta[d];
+    }
     int32_t nx[3];
-    s = cgx_cartesian_num_bins(grid_min, grid_max, grid_delta, nx);
+    s = cgx_cartesian_num_bins(gmin, gmax, gdel, nx);
     if (s) return s;
     const int64_t ncell = int64_t(nx[0]) * nx[1] * nx[2];
     if (ncell >= (int64_t(1) << 31)) return fail(CGX_ERR_NOT_SUPPORTED, "more than 2^31 bins");
     double mn[3], rdx[3];
     for (int d = 0; d < 3; ++d) {
-        mn[d] = grid_min[d];
-        const double dx = (grid_max[d] - grid_min[d]) / nx[d];
+        mn[d] = gmin[d];
+        const double dx = (gmax[d] - gmin[d]) / nx[d];
         rdx[d] = 1.0 / dx;
     }
     const int64_t n = end - begin;
@@ -1020,12 +1034,31 @@ cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions, int64
     void* scratch = p;
     CGX_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(int), st));
     CGX_CUDA(cudaMemsetAsync(counts, 0, size_t(ncell) * sizeof(int32_t), st));
-    CGX_CUDA(cartesian_keys(to_dfield(*positions), begin, end, mn, rdx, nx, keys, counts, h->flags, st, h->sms));
+    CGX_CUDA(cartesian_keys(to_dfield(*positions), dims, begin, end, mn, rdx, nx, keys, counts, h->flags, st,
+                            h->sms));
     CGX_CUDA(exclusive_scan_counts(counts, ncell, offsets, nullptr, scratch, h->sms, st));
     if (n > 0)
         CGX_CUDA(radix_sort_pairs(keys, n, key_bits_for(ncell), permutes, nullptr, uint64_t(begin), scratch,
                                   radix_sort_scratch_bytes(n), h->sms, st));
     return CGX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions, int64_t begin, int64_t end,
+                                 const double grid_min[3], const double grid_max[3], const double grid_delta[3],
+                                 int32_t* counts, uint64_t* offsets, uint64_t* permutes, void* stream) {
+    return linked_cell_build(h, positions, 3, begin, end, grid_min, grid_max, grid_delta, counts, offsets, permutes,
+                             stream);
+}
+
+cgx_status cgx_linked_cell_build_2d(cgx_handle h, const cgx_field* positions, int64_t begin, int64_t end,
+                                    const double grid_min[2], const double grid_max[2], const double grid_delta[2],
+                                    int32_t* counts, uint64_t* offsets, uint64_t* permutes, void* stream) {
+    return linked_cell_build(h, positions, 2, begin, end, grid_min, grid_max, grid_delta, counts, offsets, permutes,
+                             stream);
 }
 
 cgx_status cgx_bin_by_key(cgx_handle h, const int32_t* keys, int64_t begin, int64_t end, int32_t nbin,

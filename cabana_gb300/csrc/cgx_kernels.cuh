@@ -221,9 +221,11 @@ size_t scan_scratch_bytes(int64_t n);
 // into offsets_total (device, may be null).
 cudaError_t exclusive_scan_counts(const int32_t* counts, int64_t n, uint64_t* offsets, uint64_t* total, void* scratch,
                                   int sms, cudaStream_t st);
-cudaError_t cartesian_keys(const DField& pos, int64_t begin, int64_t end, const double* mn, const double* rdx,
-                           const int32_t* nx, uint32_t* keys, int32_t* counts, int* error_flag, cudaStream_t st,
-                           int sms);
+// Cell keys of positions with `dims` (2 or 3) coordinates; for 2 the third
+// dimension has nx[2] == 1 and is not read.
+cudaError_t cartesian_keys(const DField& pos, int dims, int64_t begin, int64_t end, const double* mn,
+                           const double* rdx, const int32_t* nx, uint32_t* keys, int32_t* counts, int* error_flag,
+                           cudaStream_t st, int sms);
 cudaError_t key_histogram(const int32_t* keys, int64_t begin, int64_t end, uint32_t* keys_out, int32_t* counts,
                           int32_t nbin, int* error_flag, cudaStream_t st, int sms);
 cudaError_t permute_field(const uint64_t* perm, int64_t begin, int64_t end, const DField& f, int ncomp, void* scratch,

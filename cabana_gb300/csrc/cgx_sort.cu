@@ -207,10 +207,12 @@ __device__ __forceinline__ void aggregated_count(int32_t* counts, int key, bool 
 }
 
 // CartesianGrid::locatePoint + cardinalCellIndex
-// (core/src/impl/Cabana_CartesianGrid.hpp:171-182, :226-231).
-__global__ void cartesian_keys_kernel(DField pos, int64_t begin, int64_t end, double mn0, double mn1, double mn2,
-                                      double r0, double r1, double r2, int nx0, int nx1, int nx2, uint32_t* keys,
-                                      int32_t* counts, int* error_flag) {
+// (core/src/impl/Cabana_CartesianGrid.hpp:171-182, :226-231; 2D :158-168,
+// :233-238). With dims == 2 the host passes nx2 == 1 and the third
+// coordinate is neither read nor binned, so the key is i * nx1 + j.
+__global__ void cartesian_keys_kernel(DField pos, int dims, int64_t begin, int64_t end, double mn0, double mn1,
+                                      double mn2, double r0, double r1, double r2, int nx0, int nx1, int nx2,
+                                      uint32_t* keys, int32_t* counts, int* error_flag) {
     const int64_t n = end - begin;
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     const int64_t nloop = (n + stride - 1) / stride * stride;
@@ -224,6 +226,10 @@ __global__ void cartesian_keys_kernel(DField pos, int64_t begin, int64_t end, do
             int c[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
+                if (d >= dims) {
+                    c[d] = 0;
+                    continue;
+                }
                 c[d] = int(floor(__dmul_rn(__dsub_rn(load_field<double>(pos, p, d), mn[d]), rdx[d])));
                 c[d] = (c[d] == nx[d]) ? c[d] - 1 : c[d];
                 // The reference indexes out of bounds here; clamp and report.
@@ -495,14 +501,15 @@ cudaError_t radix_sort_pairs(uint32_t* keys_in, int64_t n, int key_bits, uint64_
     return cudaGetLastError();
 }
 
-cudaError_t cartesian_keys(const DField& pos, int64_t begin, int64_t end, const double* mn, const double* rdx,
-                           const int32_t* nx, uint32_t* keys, int32_t* counts, int* error_flag, cudaStream_t st,
-                           int sms) {
+cudaError_t cartesian_keys(const DField& pos, int dims, int64_t begin, int64_t end, const double* mn,
+                           const double* rdx, const int32_t* nx, uint32_t* keys, int32_t* counts, int* error_flag,
+                           cudaStream_t st, int sms) {
     const int64_t n = end - begin;
     if (n <= 0) return cudaSuccess;
-    cartesian_keys_kernel<<<blocks_for(n, 256, sms), 256, 0, st>>>(pos, begin, end, mn[0], mn[1], mn[2], rdx[0],
-                                                                    rdx[1], rdx[2], nx[0], nx[1], nx[2], keys,
-                                                                    counts, error_flag);
+    if ((dims != 2 && dims != 3) || (dims == 2 && nx[2] != 1)) return cudaErrorInvalidValue;
+    cartesian_keys_kernel<<<blocks_for(n, 256, sms), 256, 0, st>>>(pos, dims, begin, end, mn[0], mn[1], mn[2],
+                                                                    rdx[0], rdx[1], rdx[2], nx[0], nx[1], nx[2],
+                                                                    keys, counts, error_flag);
     return cudaGetLastError();
 }
 

@@ -391,6 +391,22 @@ cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions,
                                  uint64_t* offsets, uint64_t* permutes,
                                  void* stream);
 
+/*
+ * The same for LinkedCellList<MemorySpace, Scalar, 2> (2D positions (p, 0..1),
+ * core/src/Cabana_LinkedCellList.hpp:652-745 with
+ * core/src/impl/Cabana_CartesianGrid.hpp's 2D locatePoint :158-168 and
+ * cardinalCellIndex :233-238, i * nbin[1] + j). counts / offsets hold
+ * nbin[0] * nbin[1] bins; nbin[d] = floor((grid_max[d] - grid_min[d]) /
+ * grid_delta[d]) as in cgx_cartesian_num_bins.
+ */
+cgx_status cgx_linked_cell_build_2d(cgx_handle h, const cgx_field* positions,
+                                    int64_t begin, int64_t end,
+                                    const double grid_min[2],
+                                    const double grid_max[2],
+                                    const double grid_delta[2],
+                                    int32_t* counts, uint64_t* offsets,
+                                    uint64_t* permutes, void* stream);
+
 /* binByKey(keys, nbin, begin, end) (core/src/Cabana_Sort.hpp:164-226) with
  * a stable in-bin order: keys[begin..end) in [0, nbin). */
 cgx_status cgx_bin_by_key(cgx_handle h, const int32_t* keys, int64_t begin,

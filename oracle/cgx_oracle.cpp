@@ -792,28 +792,32 @@ void oracle_cartesian_num_bins(const double* grid_min, const double* grid_max,
         nbin[d] = static_cast<int32_t>(std::floor((grid_max[d] - grid_min[d]) * (1.0 / grid_delta[d])));
 }
 
-// LinkedCellList::build, Cabana_LinkedCellList.hpp:652-745, run serially so
-// that particles inside a bin keep ascending index order.
-void oracle_linked_cell_build(const double* positions, int64_t begin, int64_t end,
-                              const double* grid_min, const double* grid_max,
-                              const double* grid_delta, int32_t* counts, uint64_t* offsets,
-                              uint64_t* permutes) {
-    int32_t nx[3];
-    double dx[3], rdx[3];
-    oracle_cartesian_num_bins(grid_min, grid_max, grid_delta, nx);
-    for (int d = 0; d < 3; ++d) {
-        dx[d] = (grid_max[d] - grid_min[d]) / nx[d];
-        rdx[d] = 1.0 / dx[d];
+// LinkedCellList<..., nd>::build, Cabana_LinkedCellList.hpp:652-745, for nd
+// = 2 or 3 coordinates per point (positions[nd * p + d]; grid arrays with nd
+// entries), run serially so that particles inside a bin keep ascending index
+// order.
+void oracle_linked_cell_build_nd(int nd, const double* positions, int64_t begin, int64_t end,
+                                 const double* grid_min, const double* grid_max,
+                                 const double* grid_delta, int32_t* counts, uint64_t* offsets,
+                                 uint64_t* permutes) {
+    int32_t nx[3] = {1, 1, 1};
+    double rdx[3] = {1.0, 1.0, 1.0};
+    for (int d = 0; d < nd; ++d) {
+        // CartesianGrid::init, Cabana_CartesianGrid.hpp:61-73
+        nx[d] = static_cast<int32_t>(std::floor((grid_max[d] - grid_min[d]) * (1.0 / grid_delta[d])));
+        const double dx = (grid_max[d] - grid_min[d]) / nx[d];
+        rdx[d] = 1.0 / dx;
     }
     const int64_t ncell = int64_t(nx[0]) * nx[1] * nx[2];
     auto cell_of = [&](int64_t p) {
-        int c[3];
-        for (int d = 0; d < 3; ++d) {
-            // locatePoint, CartesianGrid.hpp:171-182
-            c[d] = static_cast<int>(std::floor((positions[3 * p + d] - grid_min[d]) * rdx[d]));
+        int c[3] = {0, 0, 0};
+        for (int d = 0; d < nd; ++d) {
+            // locatePoint, CartesianGrid.hpp:171-182 (2D :158-168)
+            c[d] = static_cast<int>(std::floor((positions[nd * p + d] - grid_min[d]) * rdx[d]));
             c[d] = (c[d] == nx[d]) ? c[d] - 1 : c[d];
         }
-        // cardinalCellIndex, CartesianGrid.hpp:226-231
+        // cardinalCellIndex, CartesianGrid.hpp:226-231; in 2D (:233-238)
+        // i * nx[1] + j, the same number with nx[2] == 1 and c[2] == 0
         return (int64_t(c[0]) * nx[1] + c[1]) * nx[2] + c[2];
     };
     std::fill(counts, counts + ncell, 0);
@@ -828,6 +832,14 @@ void oracle_linked_cell_build(const double* positions, int64_t begin, int64_t en
         int64_t c = cell_of(p);
         permutes[offsets[c] + fill[c]++] = uint64_t(p);
     }
+}
+
+void oracle_linked_cell_build(const double* positions, int64_t begin, int64_t end,
+                              const double* grid_min, const double* grid_max,
+                              const double* grid_delta, int32_t* counts, uint64_t* offsets,
+                              uint64_t* permutes) {
+    oracle_linked_cell_build_nd(3, positions, begin, end, grid_min, grid_max, grid_delta, counts,
+                                offsets, permutes);
 }
 
 void oracle_bin_by_key(const int32_t* keys, int64_t begin, int64_t end, int32_t nbin,

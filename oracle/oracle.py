@@ -273,17 +273,22 @@ def cartesian_num_bins(grid_min, grid_max, grid_delta):
 
 
 def linked_cell_build(positions, begin, end, grid_min, grid_max, grid_delta):
-    positions = np.ascontiguousarray(positions, np.float64)
+    """LinkedCellList<..., nd>::build with nd = len(grid_min) (2 or 3);
+    positions are (n, nd). Returns (nbin[nd], counts, offsets, permutes)."""
     mn, mx, dl = (np.ascontiguousarray(v, np.float64) for v in (grid_min, grid_max, grid_delta))
-    nb = cartesian_num_bins(mn, mx, dl)
+    nd = mn.shape[0]
+    assert nd in (2, 3) and mx.shape[0] == nd and dl.shape[0] == nd
+    positions = np.ascontiguousarray(positions, np.float64).reshape(-1, nd)
+    nb = np.floor((mx - mn) * (1.0 / dl)).astype(np.int32) if nd == 2 else cartesian_num_bins(mn, mx, dl)
     ncell = int(np.prod(nb.astype(np.int64)))
     counts = np.zeros(ncell, np.int32)
     offsets = np.zeros(ncell, np.uint64)
     permutes = np.zeros(end - begin, np.uint64)
     u64 = ctypes.POINTER(ctypes.c_uint64)
-    lib().oracle_linked_cell_build(_dp(positions), ctypes.c_int64(begin), ctypes.c_int64(end), _dp(mn), _dp(mx),
-                                   _dp(dl), counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                                   offsets.ctypes.data_as(u64), permutes.ctypes.data_as(u64))
+    lib().oracle_linked_cell_build_nd(ctypes.c_int(nd), _dp(positions), ctypes.c_int64(begin), ctypes.c_int64(end),
+                                      _dp(mn), _dp(mx), _dp(dl),
+                                      counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                      offsets.ctypes.data_as(u64), permutes.ctypes.data_as(u64))
     return nb, counts, offsets, permutes
 
 

@@ -109,3 +109,8 @@ def test_argument_checks_fail_loudly(lib):
     mesh4 = L.make_mesh(mp)
     mesh4.num_space_dim = 4
     assert lib.cgx_tiling_init(ctypes.byref(mesh4), 2, (ctypes.c_int32 * 3)(8, 8, 8), ctypes.byref(t)) == L.CGX_ERR_INVALID_ARG
+    d2 = ctypes.c_double * 2
+    st = lib.cgx_linked_cell_build_2d(None, ctypes.byref(pts), 0, 1, d2(0, 0), d2(1, 1), d2(1, 1), None, None, None,
+                                      None)
+    assert st == L.CGX_ERR_INVALID_ARG
+    assert b"handle" in lib.cgx_last_error()

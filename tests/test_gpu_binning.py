@@ -56,6 +56,55 @@ def test_linked_cell_list_reference_case(oracle, begin, end):
                     pid += 1
 
 
+@pytest.mark.parametrize("begin,end", [(0, 100), (25, 75)])
+def test_linked_cell_list_2d_reference_case(oracle, begin, end):
+    """tstLinkedCellList.hpp's 2D case (LCLTestData<2>, checkLinkedCell
+    :366-440) on the GPU: 10^2 unit cells, one particle per cell centre."""
+    pos = np.array([(i + 0.5, j + 0.5) for j in range(NX) for i in range(NX)])
+    ids = np.array([(i, j) for j in range(NX) for i in range(NX)], np.float64)
+    tpos = torch.tensor(pos, device="cuda")
+    tids = torch.tensor(ids, device="cuda")
+    lcl = C.createLinkedCellList(tpos, (1.0, 1.0), (0.0, 0.0), (10.0, 10.0), begin, end)
+    assert lcl.totalBins() == 100 and lcl.numBin(0) == 10 and lcl.numBin(1) == 10
+    nb, counts, offsets, permutes = oracle.linked_cell_build(pos, begin, end, (0, 0), (10, 10), (1, 1))
+    bd = lcl.binningData()
+    assert np.array_equal(bd.counts.cpu().numpy(), counts)
+    assert np.array_equal(bd.offsets.cpu().numpy().astype(np.uint64), offsets)
+    assert np.array_equal(bd.permutes.cpu().numpy().astype(np.uint64), permutes)
+    C.permute(lcl, tpos, tids)
+    sorted_ids = ids.copy()
+    oracle.permute(permutes, begin, end, sorted_ids)
+    assert np.array_equal(tids.cpu().numpy(), sorted_ids)
+    pid = 0
+    for i in range(NX):
+        for j in range(NX):
+            if begin <= i + j * NX < end:
+                assert tuple(sorted_ids[begin + pid].astype(int)) == (i, j)
+                assert lcl.binSize(i, j) == 1 and lcl.binSize((i, j)) == 1
+                assert lcl.binOffset(i, j) == pid
+                pid += 1
+
+
+@pytest.mark.parametrize("n,clumps", [(1, 0), (5000, 0), (200000, 2)])
+def test_linked_cell_2d_random_bit_exact(oracle, n, clumps):
+    rng = np.random.default_rng(70 + n)
+    lo, hi = (0.0, -1.0), (6.3, 5.0)
+    if clumps:
+        centres = rng.uniform(lo, hi, size=(clumps, 2))
+        pos = centres[rng.integers(0, clumps, n)] + rng.normal(0.0, 0.05, size=(n, 2))
+        pos = np.clip(pos, lo, np.nextafter(np.array(hi), -np.inf))
+    else:
+        pos = rng.uniform(lo, hi, size=(n, 2))
+    delta = (0.37, 0.5)
+    nb, counts, offsets, permutes = oracle.linked_cell_build(pos, 0, n, lo, hi, delta)
+    lcl = C.createLinkedCellList(torch.tensor(pos, device="cuda"), delta, lo, hi)
+    assert (lcl.numBin(0), lcl.numBin(1)) == tuple(nb)
+    bd = lcl.binningData()
+    assert np.array_equal(bd.counts.cpu().numpy(), counts)
+    assert np.array_equal(bd.offsets.cpu().numpy().astype(np.uint64), offsets)
+    assert np.array_equal(bd.permutes.cpu().numpy().astype(np.uint64), permutes)
+
+
 @pytest.mark.parametrize("n,clumps", [(1, 0), (5000, 0), (200000, 2), (300000, 1)])
 def test_linked_cell_random_bit_exact(oracle, n, clumps):
     rng = np.random.default_rng(n)

@@ -3,6 +3,8 @@
 * core/unit_test/tstLinkedCellList.hpp:26-440: a 10^3 grid of unit cells,
   one particle per cell centre, created i-fastest so the binned order
   (i slowest, k fastest) reverses it; full and partial (250..750) ranges.
+  The 2D twin (LCLTestData<2>, :108-175, checkLinkedCell :366-440): a 10^2
+  grid, 100 particles, full and partial (25..75) ranges.
 * core/unit_test/tstSort.hpp:60-200: reversed keys give a reversed
   permutation.
 """
@@ -52,6 +54,56 @@ def test_linked_cell_list(oracle, begin, end):
                     assert tuple(sorted_ids[n].astype(int)) == (i, j, k)
                     assert counts[i, j, k] == 0
                 n += 1
+
+
+def lcl_particles_2d():
+    pos = np.zeros((NX ** 2, 2))
+    ids = np.zeros((NX ** 2, 2), np.int64)
+    for j in range(NX):
+        for i in range(NX):
+            pid = i + j * NX
+            ids[pid] = (i, j)
+            pos[pid] = (i + 0.5, j + 0.5)
+    return pos, ids
+
+
+@pytest.mark.parametrize("begin,end", [(0, 100), (25, 75)])
+def test_linked_cell_list_2d(oracle, begin, end):
+    pos, ids = lcl_particles_2d()
+    nb, counts, offsets, permutes = oracle.linked_cell_build(pos, begin, end, (0, 0), (10, 10), (1, 1))
+    assert tuple(nb) == (10, 10)
+    counts = counts.reshape(NX, NX)
+    offsets = offsets.reshape(NX, NX)
+    sorted_ids = ids.astype(np.float64).copy()
+    oracle.permute(permutes, begin, end, sorted_ids)
+    pid = 0
+    for i in range(NX):
+        for j in range(NX):
+            orig = i + j * NX
+            if begin <= orig < end:
+                assert tuple(sorted_ids[begin + pid].astype(int)) == (i, j)
+                assert counts[i, j] == 1
+                assert offsets[i, j] == pid
+                pid += 1
+    n = 0
+    for j in range(NX):
+        for i in range(NX):
+            if not (begin <= n < end):
+                assert tuple(sorted_ids[n].astype(int)) == (i, j)
+                assert counts[i, j] == 0
+            n += 1
+
+
+def test_linked_cell_2d_is_3d_with_one_z_cell(oracle):
+    """2D keys i * ny + j equal the 3D keys of the same points with a single
+    z cell, so the 2D build equals the 3D build with a constant z."""
+    rng = np.random.default_rng(12)
+    pos = rng.uniform((0.0, -1.0), (3.7, 2.0), size=(4000, 2))
+    nb2, c2, o2, p2 = oracle.linked_cell_build(pos, 100, 3900, (0.0, -1.0), (3.7, 2.0), (0.31, 0.23))
+    pos3 = np.concatenate([pos, np.full((4000, 1), 0.5)], axis=1)
+    nb3, c3, o3, p3 = oracle.linked_cell_build(pos3, 100, 3900, (0.0, -1.0, 0.0), (3.7, 2.0, 1.0), (0.31, 0.23, 1.0))
+    assert tuple(nb3) == tuple(nb2) + (1,)
+    assert np.array_equal(c2, c3) and np.array_equal(o2, o3) and np.array_equal(p2, p3)
 
 
 def test_bin_by_key_reversed(oracle):
