@@ -232,7 +232,9 @@ __global__ void cartesian_keys_kernel(DField pos, int dims, int64_t begin, int64
                 }
                 c[d] = int(floor(__dmul_rn(__dsub_rn(load_field<double>(pos, p, d), mn[d]), rdx[d])));
                 c[d] = (c[d] == nx[d]) ? c[d] - 1 : c[d];
-                // The reference indexes out of bounds here; clamp and report.
+                // The reference indexes out of bounds here: clamp to the edge
+                // bin and set the flag word (the linked-cell build does not
+                // synchronise to read it back).
                 if (c[d] < 0 || c[d] >= nx[d]) {
                     raise_error(error_flag, CGX_ERR_OUT_OF_BOUNDS);
                     c[d] = c[d] < 0 ? 0 : nx[d] - 1;

@@ -381,7 +381,10 @@ cgx_status cgx_cartesian_num_bins(const double grid_min[3],
  * 652-745): counts[prod(nbin)], offsets[prod(nbin)] (exclusive scan of counts,
  * relative to `begin`), permutes[end-begin] (original indices in binned
  * order). Within a bin, particles keep ascending index order -- the order of
- * the reference's Serial backend -- so the output is deterministic.
+ * the reference's Serial backend -- so the output is deterministic. A
+ * position outside [grid_min, grid_max] (the reference indexes out of bounds
+ * there) is put in the nearest edge bin; the call stays asynchronous and
+ * does not report it.
  */
 cgx_status cgx_linked_cell_build(cgx_handle h, const cgx_field* positions,
                                  int64_t begin, int64_t end,
