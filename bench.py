@@ -71,6 +71,31 @@ def dist_info():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest x over all ranks: a job's time is its slowest rank's."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(n_per_rank, world, ms_per_step):
+    """Whole-job particles/s: every rank transfers n_per_rank particles per
+    step (replicas, weak scaling) in the slowest rank's step time."""
+    return n_per_rank * world / (ms_per_step / 1000.0)
+
+
+# DRAM bytes (read + write) of one launch of each tiled kernel, from an ncu
+# capture of the same kernels on the clumped 2^24-particle, 128^3-cell case
+# (dram__bytes_read.sum + dram__bytes_write.sum); the bench's traffic scales
+# them to its particle count (particles and nodes both grow about 8x to the
+# default 2^27 / 256^3 workload).
+NCU_TRAFFIC = {"p2g": (1297.9e6 + 15.8e6, 16777216), "g2p": (1221.6e6 + 752.0e6, 16777216)}
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -668,13 +693,9 @@ def run_ours(args):
     clocks.start()
     total_ms, p2g_ms, g2p_ms = time_steps(tr, args.steps, args.warmup, barrier)
     clk = clocks.stop()
-    t = torch.tensor([total_ms], device=dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world, dev)
     ms_per_step = total_ms / args.steps
-    value = n * world / (ms_per_step / 1000.0)
+    value = job_value(n, world, ms_per_step)
 
     p2g_avg = statistics.mean(p2g_ms)
     g2p_avg = statistics.mean(g2p_ms)
@@ -794,12 +815,12 @@ def run_ours(args):
         s1.record(s_out)
         torch.cuda.synchronize()
         barrier()
-        ems = s0.elapsed_time(s1) / esteps
+        ems = max_over_ranks(s0.elapsed_time(s1) / esteps, world, dev)
         # every buffer set processed the same inputs: their last results agree
         # up to the summation order of the grid atomics
         sets_rel = max(float((h_out[i][j] - h_out[0][j]).abs().max() / h_out[0][j].abs().max())
                        for i in range(1, nsets) for j in range(2))
-        e2e = {"value": n * world / (ems / 1000.0), "unit": "particles/s", "ms_per_step": ems,
+        e2e = {"value": job_value(n, world, ems), "unit": "particles/s", "ms_per_step": ems,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "buffer_sets_max_rel": sets_rel,
                "note": "pinned host buffers; every step: H2D of positions, mass, momentum, stress, tile sort + "
                        "permute of all particle fields, zero grids, P2G + G2P, D2H of velocity and velocity "
@@ -840,7 +861,10 @@ def run_ours(args):
                 "config": dict(workload_config(args, ext), form="FP32-compensated tiled", tile=[args.tile] * 3,
                                parallelism=f"replicas x{world}"),
                 "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+                             "frac": achieved / peak, "peak_source": peak_src,
+                             "traffic": NCU_TRAFFIC[dom[0]][0] * n / NCU_TRAFFIC[dom[0]][1],
+                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel "
+                                               "on 2^24 clumped particles / 128^3 cells, scaled by particles",
                              "algorithmic_bytes_per_launch": dom[2], "avg_launch_ms": dom[1]},
                 "step_roofline": {"algorithmic_bytes": step_bytes,
                                   "achieved_gbs": step_bytes / (ms_per_step / 1000.0) / 1e9,
