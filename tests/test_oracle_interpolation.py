@@ -7,6 +7,9 @@
 * grid/unit_test/tstSplineEvaluation3d.hpp:262-511: cell-centred points,
   Spline<1> on nodes: cell size, logical coordinates i + 0.5, stencil
   {i, i+1}, weights 0.5, gradient weights +-1/(2 dx), sum of w*d = 0.
+* The 1-D identities of grid/unit_test/tstSplines.cpp (partition of unity,
+  linear reproduction and its derivative) lifted to the 3D operators on
+  random points, Spline<0..6>: P2G moments and G2P of linear grid fields.
 """
 import numpy as np
 import pytest
@@ -129,3 +132,65 @@ def test_openmp_duplicated_scatter_matches_serial(oracle):
         oracle.p2g(om, pts, order, [(0, 1.0, m, g4)], nthreads=4)
         np.testing.assert_allclose(g4, g1, rtol=1e-13, atol=1e-13)
         assert abs(g1.sum() - m.sum()) < 1e-9 * m.sum()
+
+
+@pytest.mark.parametrize("order", [0, 1, 2, 3, 4, 5, 6])
+def test_p2g_moments_random_points(oracle, order):
+    """B-spline identities at the operator level on random (not cell-centred)
+    points: ScalarValueP2G of ones sums to the particle count (partition of
+    unity) and its node-coordinate moments give the particle positions (linear
+    reproduction, orders >= 1); ScalarGradientP2G of ones sums to zero and its
+    moments give the identity (the derivative of linear reproduction). They pin
+    which node and which dof each weight product lands on in 3D."""
+    lg, mp = M.simple_mesh((9, 7, 8), 0.3, (0.4, -1.3, 2.0), 4)
+    om = oracle.make_mesh(mp.ghost_low, mp.cell_size, mp.owned_cells, mp.halo_width, mp.periodic, mp.entity)
+    rng = np.random.default_rng(40 + order)
+    n = 2000
+    lo = np.array((0.4, -1.3, 2.0))
+    pts = lo + rng.uniform(0.0, 1.0, size=(n, 3)) * (np.array((9, 7, 8)) * 0.3)
+    ext = mp.extents()
+    coords = [np.asarray(mp.ghost_low[d]) + np.arange(ext[d]) * mp.cell_size[d] for d in range(3)]
+    X = np.stack(np.meshgrid(*coords, indexing="ij"), axis=-1)  # node coordinates (i, j, k, d)
+    ones = np.ones((n, 1))
+    value = np.zeros(ext + (1,))
+    assert oracle.p2g(om, pts, order, [(0, 1.0, ones, value)]) == 0
+    assert abs(value.sum() - n) < 1e-10 * n
+    if order >= 1:
+        moments = np.einsum("ijk,ijkd->d", value[..., 0], X)
+        np.testing.assert_allclose(moments, pts.sum(axis=0), rtol=1e-12)
+    grad = np.zeros(ext + (3,))
+    assert oracle.p2g(om, pts, order, [(2, 1.0, ones, grad)]) == 0
+    np.testing.assert_allclose(grad.sum(axis=(0, 1, 2)), 0.0, atol=1e-9 * n / 0.3)
+    if order >= 1:
+        jac = np.einsum("ijkd,ijke->de", grad, X)  # sum over particles of d x_e / d x_d
+        np.testing.assert_allclose(jac, n * np.eye(3), atol=1e-8 * n)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4, 5, 6])
+def test_g2p_reproduces_linear_fields(oracle, order):
+    """G2P of a grid field that is linear in the node coordinates, f = a . X +
+    b: ScalarValueG2P returns f(x_p) and ScalarGradientG2P returns a at every
+    random point; VectorGradientG2P of (f, 2 f, -f) returns the rows
+    (derivative index first, as Interpolation.hpp:247-282) a x (1, 2, -1)."""
+    lg, mp = M.simple_mesh((9, 7, 8), 0.3, (0.4, -1.3, 2.0), 4)
+    om = oracle.make_mesh(mp.ghost_low, mp.cell_size, mp.owned_cells, mp.halo_width, mp.periodic, mp.entity)
+    rng = np.random.default_rng(60 + order)
+    n = 1500
+    lo = np.array((0.4, -1.3, 2.0))
+    pts = lo + rng.uniform(0.0, 1.0, size=(n, 3)) * (np.array((9, 7, 8)) * 0.3)
+    ext = mp.extents()
+    coords = [np.asarray(mp.ghost_low[d]) + np.arange(ext[d]) * mp.cell_size[d] for d in range(3)]
+    X = np.stack(np.meshgrid(*coords, indexing="ij"), axis=-1)
+    a, b = np.array((0.7, -1.9, 2.6)), 0.35
+    f = (X @ a + b)[..., None]
+    val = np.zeros((n, 1))
+    assert oracle.g2p(om, pts, order, [(0, 1.0, val, f.copy())]) == 0
+    np.testing.assert_allclose(val[:, 0], pts @ a + b, rtol=1e-11, atol=1e-11)
+    grad = np.zeros((n, 3))
+    assert oracle.g2p(om, pts, order, [(2, 1.0, grad, f.copy())]) == 0
+    np.testing.assert_allclose(grad, np.broadcast_to(a, (n, 3)), rtol=1e-10, atol=1e-10)
+    fv = np.concatenate([f, 2.0 * f, -f], axis=-1)
+    vg = np.zeros((n, 9))
+    assert oracle.g2p(om, pts, order, [(3, 1.0, vg, fv)]) == 0
+    expect = np.outer(a, (1.0, 2.0, -1.0)).ravel()  # result[m][n] = sum d_m W f_n
+    np.testing.assert_allclose(vg, np.broadcast_to(expect, (n, 9)), rtol=1e-10, atol=1e-10)
