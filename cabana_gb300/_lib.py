@@ -39,7 +39,7 @@ CGX_DISPATCH_TILED = 2
 EXPORTS = (
     "cgx_create", "cgx_destroy", "cgx_last_error", "cgx_version", "cgx_last_dispatch",
     "cgx_p2g", "cgx_g2p", "cgx_g2p2g", "cgx_p2g_adjoint", "cgx_g2p_adjoint", "cgx_halo_scatter_sum", "cgx_halo_gather", "cgx_array_assign",
-    "cgx_cartesian_num_bins", "cgx_linked_cell_build", "cgx_linked_cell_build_2d", "cgx_bin_by_key", "cgx_bin_by_key_static", "cgx_permute",
+    "cgx_cartesian_num_bins", "cgx_linked_cell_build", "cgx_linked_cell_build_2d", "cgx_bin_by_key", "cgx_bin_by_key_range", "cgx_bin_by_key_static", "cgx_permute",
     "cgx_tiling_init", "cgx_tiling_num_offsets", "cgx_sort_tiles",
     "cgx_batch_plan_create", "cgx_batch_plan_destroy", "cgx_batch_execute", "cgx_batch_autotune",
     "cgx_batch_get_config", "cgx_batch_set_config",
@@ -175,6 +175,8 @@ def lib():
     L.cgx_linked_cell_build_2d.argtypes = [vp, P(CgxField), ctypes.c_int64, ctypes.c_int64, d2, d2, d2, vp, vp, vp,
                                            vp]
     L.cgx_bin_by_key.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, vp, vp, vp, vp]
+    L.cgx_bin_by_key_range.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int, vp, vp,
+                                        vp, vp]
     L.cgx_bin_by_key_static.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, vp, vp, vp, vp]
     L.cgx_permute.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int64, P(CgxField), P(ctypes.c_int32), ctypes.c_int, vp]
     L.cgx_tiling_init.argtypes = [P(CgxMesh), ctypes.c_int, ctypes.c_int32 * 3, P(CgxTiling)]

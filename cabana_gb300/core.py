@@ -2,7 +2,8 @@
 
   LinkedCellList / createLinkedCellList  (core/src/Cabana_LinkedCellList.hpp:128-1146)
   BinningData                           (core/src/Cabana_Sort.hpp:37-136)
-  binByKey                              (core/src/Cabana_Sort.hpp:164-226)
+  binByKey / sortByKey                  (core/src/Cabana_Sort.hpp:217-235, :364-443)
+  binByIndex (keys are bin numbers)     (the BinSort of core/src/Cabana_Sort.hpp:164-182)
   permute                               (core/src/Cabana_Sort.hpp:549-720)
 
 All work runs in libcgx.so. Bins keep particles in ascending index order
@@ -120,7 +121,46 @@ def createLinkedCellList(positions, grid_delta, grid_min, grid_max, begin=0, end
     return LinkedCellList(positions, grid_delta, grid_min, grid_max, begin, end, **kw)
 
 
+def _int_keys(keys):
+    if keys.dtype.is_floating_point or keys.dtype == torch.bool:
+        raise TypeError("keys must be an integer tensor (values within int32)")
+    return keys.to(torch.int32).contiguous()
+
+
+def _bin_range(keys, nbin, begin, end, sort_within_bins, handle, stream):
+    end = keys.shape[0] if end is None else end
+    if nbin < 0:
+        raise ValueError("nbin must be >= 0")
+    keys = _int_keys(keys)
+    counts = torch.zeros(nbin + 1, dtype=torch.int32, device=keys.device)
+    offsets = torch.zeros(nbin + 1, dtype=torch.int64, device=keys.device)
+    permutes = torch.zeros(max(1, end - begin), dtype=torch.int64, device=keys.device)
+    h = handle or L.default_handle()
+    L.check(L.lib().cgx_bin_by_key_range(h.ptr, ctypes.c_void_p(keys.data_ptr()), begin, end, nbin,
+                                         1 if sort_within_bins else 0, ctypes.c_void_p(counts.data_ptr()),
+                                         ctypes.c_void_p(offsets.data_ptr()), ctypes.c_void_p(permutes.data_ptr()),
+                                         _stream(stream)))
+    return BinningData(begin, end, counts, offsets, permutes[: end - begin])
+
+
 def binByKey(keys, nbin, begin=0, end=None, handle=None, stream=None):
+    """Cabana::binByKey (core/src/Cabana_Sort.hpp:411-443): nbin + 1 bins
+    splitting [min, max] of keys[begin, end) evenly (Kokkos::BinOp1D; one key
+    value per bin when max - min <= nbin); stable order inside a bin."""
+    return _bin_range(keys, nbin, begin, end, False, handle, stream)
+
+
+def sortByKey(keys, begin=0, end=None, handle=None, stream=None):
+    """Cabana::sortByKey (core/src/Cabana_Sort.hpp:364-393): BinOp1D bins with
+    nbin = (end - begin) // 2, entries ordered by key inside each bin (so the
+    permutation sorts by key; equal keys keep index order)."""
+    end = keys.shape[0] if end is None else end
+    return _bin_range(keys, (end - begin) // 2, begin, end, True, handle, stream)
+
+
+def binByIndex(keys, nbin, begin=0, end=None, handle=None, stream=None):
+    """Bins given by number: keys[begin, end) in [0, nbin), nbin bins, stable
+    order inside a bin (no reference counterpart; cgx_bin_by_key)."""
     end = keys.shape[0] if end is None else end
     counts = torch.zeros(nbin, dtype=torch.int32, device=keys.device)
     offsets = torch.zeros(nbin, dtype=torch.int64, device=keys.device)

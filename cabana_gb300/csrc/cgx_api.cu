@@ -1088,6 +1088,51 @@ cgx_status cgx_bin_by_key(cgx_handle h, const int32_t* keys, int64_t begin, int6
     return finish_check(h, CGX_FLAG_CHECK_BOUNDS, st);
 }
 
+cgx_status cgx_bin_by_key_range(cgx_handle h, const int32_t* keys, int64_t begin, int64_t end, int32_t nbin,
+                                int sort_within_bins, int32_t* counts, uint64_t* offsets, uint64_t* permutes,
+                                void* stream) {
+    if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");
+    if (begin < 0 || end < begin) return fail(CGX_ERR_INVALID_ARG, "need 0 <= begin <= end");
+    if (nbin < 0 || nbin == INT32_MAX) return fail(CGX_ERR_INVALID_ARG, "need 0 <= nbin < 2^31 - 1");
+    if ((!keys || !permutes) && end > begin) return fail(CGX_ERR_INVALID_ARG, "NULL keys / permutes");
+    if (!counts || !offsets) return fail(CGX_ERR_INVALID_ARG, "NULL output");
+    if (end - begin >= (int64_t(1) << 32)) return fail(CGX_ERR_NOT_SUPPORTED, "more than 2^32 - 1 keys");
+    const int64_t n = end - begin;
+    const int32_t nbins = nbin + 1;  // Kokkos::BinOp1D::max_bins
+    const size_t need = size_t(n) * 4 + 256 + 256 + radix_sort_scratch_bytes(n) + scan_scratch_bytes(nbins) + 1024;
+    cgx_status s = ensure_ws(h, need);
+    if (s) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    char* p = reinterpret_cast<char*>(h->ws);
+    uint32_t* k32 = reinterpret_cast<uint32_t*>(p);
+    p = align256(p + size_t(n) * 4);
+    int* minmax = reinterpret_cast<int*>(p);
+    p = align256(p + 2 * sizeof(int));
+    void* scratch = p;
+    CGX_CUDA(cudaMemsetAsync(counts, 0, size_t(nbins) * sizeof(int32_t), st));
+    if (n == 0) {
+        CGX_CUDA(exclusive_scan_counts(counts, nbins, offsets, nullptr, scratch, h->sms, st));
+        return CGX_OK;
+    }
+    // The key range sets the bin width, so it is read back first (the
+    // reference's keyMinMax is a blocking reduction too).
+    CGX_CUDA(key_minmax(keys, begin, end, minmax, st, h->sms));
+    int mm[2] = {0, 0};
+    CGX_CUDA(cudaMemcpyAsync(mm, minmax, sizeof(mm), cudaMemcpyDeviceToHost, st));
+    CGX_CUDA(cudaStreamSynchronize(st));
+    // Kokkos::BinOp1D(nbin, min, max) for integer keys: nbin / (max - min)
+    // keys per bin, or one key value per bin when the range is at most nbin.
+    const double range = double(mm[1]) - double(mm[0]);
+    const double mul = range <= double(nbin) ? 1.0 : double(nbin) / range;
+    const bool by_key = sort_within_bins != 0;
+    CGX_CUDA(key_bin1d(keys, begin, end, mm[0], mul, nbins, by_key, k32, counts, st, h->sms));
+    CGX_CUDA(exclusive_scan_counts(counts, nbins, offsets, nullptr, scratch, h->sms, st));
+    const int bits = by_key ? key_bits_for(int64_t(mm[1]) - int64_t(mm[0]) + 1) : key_bits_for(nbins);
+    CGX_CUDA(radix_sort_pairs(k32, n, bits, permutes, nullptr, uint64_t(begin), scratch, radix_sort_scratch_bytes(n),
+                              h->sms, st));
+    return CGX_OK;
+}
+
 cgx_status cgx_permute(cgx_handle h, const uint64_t* permutes, int64_t begin, int64_t end, const cgx_field* fields,
                        const int32_t* ncomps, int n_fields, void* stream) {
     if (!h) return fail(CGX_ERR_INVALID_ARG, "handle is NULL");

@@ -228,6 +228,13 @@ cudaError_t cartesian_keys(const DField& pos, int dims, int64_t begin, int64_t e
                            cudaStream_t st, int sms);
 cudaError_t key_histogram(const int32_t* keys, int64_t begin, int64_t end, uint32_t* keys_out, int32_t* counts,
                           int32_t nbin, int* error_flag, cudaStream_t st, int sms);
+// minmax[0..1] = min and max of keys[begin, end) ((INT_MAX, INT_MIN) when
+// the range is empty).
+cudaError_t key_minmax(const int32_t* keys, int64_t begin, int64_t end, int* minmax, cudaStream_t st, int sms);
+// Kokkos::BinOp1D bins of keys[begin, end) counted into counts[nbins]; the
+// sort key is the bin, or key - kmin when by_key.
+cudaError_t key_bin1d(const int32_t* keys, int64_t begin, int64_t end, int kmin, double mul, int32_t nbins, bool by_key,
+                      uint32_t* keys_out, int32_t* counts, cudaStream_t st, int sms);
 cudaError_t permute_field(const uint64_t* perm, int64_t begin, int64_t end, const DField& f, int ncomp, void* scratch,
                           cudaStream_t st, int sms);
 cudaError_t tile_keys(const DMesh& mesh, const DField& pts, int64_t n, int order, const int32_t* tile,

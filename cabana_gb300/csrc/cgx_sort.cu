@@ -7,6 +7,8 @@
 // backends. Here the permutation comes from a stable sort, so particles inside
 // a bin keep ascending index order -- the reference's Serial-backend order --
 // and the result is bit-reproducible.
+#include <climits>
+
 #include "cgx_kernels.cuh"
 
 namespace cgx {
@@ -267,6 +269,58 @@ __global__ void key_hist_kernel(const int32_t* keys, int64_t begin, int64_t end,
     }
 }
 
+// Minimum and maximum of keys[begin, end) into minmax[0..1] (the reference's
+// Impl::keyMinMax, core/src/Cabana_Sort.hpp:186-212), which the host set to
+// (INT_MAX, INT_MIN): warp shuffles, then one atomic pair per warp.
+__global__ void key_minmax_init_kernel(int* minmax) {
+    minmax[0] = INT_MAX;
+    minmax[1] = INT_MIN;
+}
+
+__global__ void key_minmax_kernel(const int32_t* keys, int64_t begin, int64_t end, int* minmax) {
+    const int64_t n = end - begin;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    int lo = INT_MAX, hi = INT_MIN;
+    for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int k = keys[begin + t];
+        lo = k < lo ? k : lo;
+        hi = k > hi ? k : hi;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const int l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0 && lo <= hi) {
+        atomicMin(minmax, lo);
+        atomicMax(minmax + 1, hi);
+    }
+}
+
+// Kokkos::BinOp1D::bin of keys[begin, end): bin = int(mul * (key - kmin)),
+// kept inside [0, nbins) against rounding, and counted per bin. The sort key
+// written to keys_out is the bin, or key - kmin when the entries are also
+// ordered by key inside their bins (bins grow with the key, so a stable sort
+// by key - kmin orders by bin, then key, then index).
+__global__ void key_bin1d_kernel(const int32_t* keys, int64_t begin, int64_t end, int kmin, double mul, int32_t nbins,
+                                 int by_key, uint32_t* keys_out, int32_t* counts) {
+    const int64_t n = end - begin;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    const int64_t nloop = (n + stride - 1) / stride * stride;
+    for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < nloop; t += stride) {
+        const bool valid = t < n;
+        int bin = 0;
+        if (valid) {
+            const int k = keys[begin + t];
+            bin = int(mul * (double(k) - double(kmin)));
+            bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+            keys_out[t] = by_key ? uint32_t(int64_t(k) - int64_t(kmin)) : uint32_t(bin);
+        }
+        aggregated_count(counts, bin, valid);
+    }
+}
+
 // One thread per element: neighbouring lanes move the components of one
 // particle, so the gathers read whole particles and the scratch copy is
 // written and read contiguously. The element -> (particle, component) split
@@ -512,6 +566,23 @@ cudaError_t cartesian_keys(const DField& pos, int dims, int64_t begin, int64_t e
     cartesian_keys_kernel<<<blocks_for(n, 256, sms), 256, 0, st>>>(pos, dims, begin, end, mn[0], mn[1], mn[2],
                                                                     rdx[0], rdx[1], rdx[2], nx[0], nx[1], nx[2],
                                                                     keys, counts, error_flag);
+    return cudaGetLastError();
+}
+
+cudaError_t key_minmax(const int32_t* keys, int64_t begin, int64_t end, int* minmax, cudaStream_t st, int sms) {
+    key_minmax_init_kernel<<<1, 1, 0, st>>>(minmax);
+    const int64_t n = end - begin;
+    if (n > 0) key_minmax_kernel<<<blocks_for(n, 256, sms), 256, 0, st>>>(keys, begin, end, minmax);
+    return cudaGetLastError();
+}
+
+cudaError_t key_bin1d(const int32_t* keys, int64_t begin, int64_t end, int kmin, double mul, int32_t nbins, bool by_key,
+                      uint32_t* keys_out, int32_t* counts, cudaStream_t st, int sms) {
+    const int64_t n = end - begin;
+    if (n <= 0) return cudaSuccess;
+    if (nbins < 1) return cudaErrorInvalidValue;
+    key_bin1d_kernel<<<blocks_for(n, 256, sms), 256, 0, st>>>(keys, begin, end, kmin, mul, nbins, by_key ? 1 : 0,
+                                                               keys_out, counts);
     return cudaGetLastError();
 }
 

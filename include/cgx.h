@@ -410,11 +410,33 @@ cgx_status cgx_linked_cell_build_2d(cgx_handle h, const cgx_field* positions,
                                     int32_t* counts, uint64_t* offsets,
                                     uint64_t* permutes, void* stream);
 
-/* binByKey(keys, nbin, begin, end) (core/src/Cabana_Sort.hpp:164-226) with
- * a stable in-bin order: keys[begin..end) in [0, nbin). */
+/* Binning by bin index: keys[begin..end) are bin numbers in [0, nbin),
+ * counts[nbin], offsets[nbin], permutes[end-begin], stable in-bin order. The
+ * BinSort of core/src/Cabana_Sort.hpp:164-182 with the identity as the bin
+ * map (the tiled kernels' tile ordering uses the same sort); a key outside
+ * [0, nbin) returns CGX_ERR_INVALID_ARG. */
 cgx_status cgx_bin_by_key(cgx_handle h, const int32_t* keys, int64_t begin,
                           int64_t end, int32_t nbin, int32_t* counts,
                           uint64_t* offsets, uint64_t* permutes, void* stream);
+
+/*
+ * Cabana::binByKey(keys, nbin, begin, end) (sort_within_bins = 0) and
+ * Cabana::sortByKey(keys, begin, end) (nbin = (end - begin) / 2,
+ * sort_within_bins = 1) over int keys (core/src/Cabana_Sort.hpp:217-235,
+ * :364-443): Kokkos::BinOp1D splits [min, max] of keys[begin..end) into
+ * nbin + 1 bins, bin = int(mul * (key - min)) with mul = nbin / (max - min),
+ * or 1 when max - min <= nbin. counts and offsets hold nbin + 1 entries;
+ * permutes[end-begin] lists the entries by bin, then (sort_within_bins) by
+ * key, then by index -- a deterministic instance of the reference's order,
+ * whose in-bin order the parallel backends leave open. Reads the key range
+ * back to the host, so the call synchronises `stream` (as the reference's
+ * key reduction blocks) and cannot be captured in a CUDA graph.
+ */
+cgx_status cgx_bin_by_key_range(cgx_handle h, const int32_t* keys,
+                                int64_t begin, int64_t end, int32_t nbin,
+                                int sort_within_bins, int32_t* counts,
+                                uint64_t* offsets, uint64_t* permutes,
+                                void* stream);
 
 /*
  * cgx_bin_by_key without any device allocation (no counterpart in the

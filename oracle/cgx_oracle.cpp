@@ -842,6 +842,47 @@ void oracle_linked_cell_build(const double* positions, int64_t begin, int64_t en
                                 offsets, permutes);
 }
 
+// Cabana::binByKey / sortByKey over int keys (core/src/Cabana_Sort.hpp:217-235
+// Impl::kokkosBinSort1d, :364-443). The bin map is Kokkos::BinOp1D, from
+// Kokkos (an external dependency of the reference, >= 4.1, not vendored):
+// max_bins = nbin + 1, mul = nbin / (max - min) over keys[begin, end), or 1
+// for integer keys when max - min <= nbin, bin = int(mul * (key - min)). The
+// BinSort order is by bin, then (sort_within_bins) by key; entries that tie
+// keep ascending index order (the serial order). counts / offsets: nbin + 1.
+void oracle_bin_by_key_range(const int32_t* keys, int64_t begin, int64_t end, int32_t nbin,
+                             int sort_within_bins, int32_t* counts, uint64_t* offsets,
+                             uint64_t* permutes) {
+    const int64_t nbins = int64_t(nbin) + 1;
+    std::fill(counts, counts + nbins, 0);
+    std::fill(offsets, offsets + nbins, uint64_t(0));
+    if (end <= begin) return;
+    int32_t kmin = keys[begin], kmax = keys[begin];
+    for (int64_t p = begin; p < end; ++p) {
+        kmin = std::min(kmin, keys[p]);
+        kmax = std::max(kmax, keys[p]);
+    }
+    const double range = static_cast<double>(kmax) - static_cast<double>(kmin);
+    const double mul = range <= static_cast<double>(nbin) ? 1.0 : static_cast<double>(nbin) / range;
+    auto bin_of = [&](int64_t p) {
+        return static_cast<int>(mul * (static_cast<double>(keys[p]) - static_cast<double>(kmin)));
+    };
+    for (int64_t p = begin; p < end; ++p) counts[bin_of(p)] += 1;
+    uint64_t run = 0;
+    for (int64_t b = 0; b < nbins; ++b) {
+        offsets[b] = run;
+        run += counts[b];
+    }
+    std::vector<int64_t> order;
+    order.reserve(size_t(end - begin));
+    for (int64_t p = begin; p < end; ++p) order.push_back(p);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+        const int ba = bin_of(a), bb = bin_of(b);
+        if (ba != bb) return ba < bb;
+        return sort_within_bins ? keys[a] < keys[b] : false;
+    });
+    for (size_t q = 0; q < order.size(); ++q) permutes[q] = uint64_t(order[q]);
+}
+
 void oracle_bin_by_key(const int32_t* keys, int64_t begin, int64_t end, int32_t nbin,
                        int32_t* counts, uint64_t* offsets, uint64_t* permutes) {
     std::fill(counts, counts + nbin, 0);

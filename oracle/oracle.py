@@ -292,6 +292,23 @@ def linked_cell_build(positions, begin, end, grid_min, grid_max, grid_delta):
     return nb, counts, offsets, permutes
 
 
+def bin_by_key_range(keys, nbin, begin=0, end=None, sort_within_bins=False):
+    """Cabana::binByKey (sort_within_bins False) / sortByKey (True, with nbin =
+    (end - begin) // 2) over int keys: nbin + 1 Kokkos::BinOp1D bins over the
+    keys' [min, max]. Returns (counts, offsets, permutes)."""
+    keys = np.ascontiguousarray(keys, np.int32)
+    end = keys.shape[0] if end is None else end
+    counts = np.zeros(nbin + 1, np.int32)
+    offsets = np.zeros(nbin + 1, np.uint64)
+    permutes = np.zeros(end - begin, np.uint64)
+    u64 = ctypes.POINTER(ctypes.c_uint64)
+    lib().oracle_bin_by_key_range(keys.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.c_int64(begin),
+                                  ctypes.c_int64(end), ctypes.c_int32(nbin), ctypes.c_int(1 if sort_within_bins else 0),
+                                  counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), offsets.ctypes.data_as(u64),
+                                  permutes.ctypes.data_as(u64))
+    return counts, offsets, permutes
+
+
 def bin_by_key(keys, nbin, begin=0, end=None):
     keys = np.ascontiguousarray(keys, np.int32)
     end = keys.shape[0] if end is None else end

@@ -1,5 +1,5 @@
 """GPU binning parity, bit-exact against the oracle: LinkedCellList counts,
-offsets and permutation (stable in-bin order), binByKey, permute, and the
+offsets and permutation (stable in-bin order), binning by bin number, permute, and the
 tile-major ordering used by the tiled kernels."""
 import numpy as np
 import pytest
@@ -131,17 +131,17 @@ def test_points_on_upper_boundary_go_to_last_bin(oracle):
     assert np.array_equal(lcl.binningData().permutes.cpu().numpy().astype(np.uint64), permutes)
 
 
-def test_bin_by_key(oracle):
-    """tstSort.hpp:60-200: reversed keys give the reversed permutation; plus a
-    random key set with many duplicates (stable order)."""
+def test_bin_by_index(oracle):
+    """Binning by bin number (cgx_bin_by_key): reversed keys give the reversed
+    permutation; plus a random key set with many duplicates (stable order)."""
     n = 3000
     keys = np.arange(n - 1, -1, -1, dtype=np.int32)
-    bd = C.binByKey(torch.tensor(keys, device="cuda"), n)
+    bd = C.binByIndex(torch.tensor(keys, device="cuda"), n)
     assert np.array_equal(bd.permutes.cpu().numpy(), np.arange(n - 1, -1, -1))
     rng = np.random.default_rng(2)
     keys = rng.integers(0, 37, size=50000).astype(np.int32)
     counts, offsets, permutes = oracle.bin_by_key(keys, 37, 1000, 40000)
-    bd = C.binByKey(torch.tensor(keys, device="cuda"), 37, 1000, 40000)
+    bd = C.binByIndex(torch.tensor(keys, device="cuda"), 37, 1000, 40000)
     assert np.array_equal(bd.counts.cpu().numpy(), counts)
     assert np.array_equal(bd.offsets.cpu().numpy().astype(np.uint64), offsets)
     assert np.array_equal(bd.permutes.cpu().numpy().astype(np.uint64), permutes)

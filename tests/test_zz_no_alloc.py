@@ -37,7 +37,7 @@ def test_static_scratch_binning_matches_allocating_entry_point():
     for n, nbin, begin, end in cases:
         keys = torch.tensor(rng.integers(0, nbin, size=n).astype(np.int32), device="cuda")
         counts, offsets, permutes = _static_bin(keys, nbin, begin, end)
-        ref = C.binByKey(keys, nbin, begin, end)
+        ref = C.binByIndex(keys, nbin, begin, end)
         torch.cuda.synchronize()
         assert torch.equal(counts, ref.counts)
         assert torch.equal(offsets, ref.offsets)
