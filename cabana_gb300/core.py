@@ -179,13 +179,26 @@ def _ncomp(x):
     return 1 if x.dim() == 1 else int(x[0].numel())
 
 
+def _move_descriptor(f):
+    """cgx_field for permute, which moves elements bit for bit: an integer
+    tensor travels as the float type of its element size (int32 as float32,
+    int64 as float64), as the reference permutes int members with the rest of
+    the AoSoA."""
+    if isinstance(f, torch.Tensor) and not f.dtype.is_floating_point:
+        if f.dtype == torch.bool or f.element_size() not in (4, 8):
+            raise TypeError(f"permute moves 4- or 8-byte elements; got {f.dtype}")
+        return field_descriptor(f.view(torch.float32 if f.element_size() == 4 else torch.float64))
+    return field_descriptor(f)
+
+
 def permute(binning, *fields, handle=None, stream=None):
-    """In-place permute of every field over the binning's range."""
+    """In-place permute of every field over the binning's range (float32,
+    float64, int32 or int64 tensors, or Slices)."""
     data = binning.binningData() if isinstance(binning, LinkedCellList) else binning
     if data.end == data.begin or not fields:
         return
     n = len(fields)
-    descs = (L.CgxField * n)(*[field_descriptor(f) for f in fields])
+    descs = (L.CgxField * n)(*[_move_descriptor(f) for f in fields])
     nc = (ctypes.c_int32 * n)(*[_ncomp(f) for f in fields])
     h = handle or L.default_handle()
     L.check(L.lib().cgx_permute(h.ptr, ctypes.c_void_p(data.permutes.data_ptr()), data.begin, data.end, descs, nc, n,

@@ -465,6 +465,9 @@ cgx_status cgx_bin_by_key_static(const int32_t* keys, int64_t begin,
  * permute(BinningData, AoSoA/Slice/View) (core/src/Cabana_Sort.hpp:549-720):
  * for each field, element i in [begin, end) becomes old element
  * permutes[i - begin], all components (ncomps[f] of them) moved together.
+ * Elements are moved bit for bit, so a field's dtype only gives the element
+ * size: CGX_F32 for any 4-byte member (float, int32), CGX_F64 for any 8-byte
+ * member (double, int64).
  */
 cgx_status cgx_permute(cgx_handle h, const uint64_t* permutes, int64_t begin,
                        int64_t end, const cgx_field* fields,

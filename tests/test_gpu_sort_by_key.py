@@ -7,6 +7,7 @@ stable order inside a bin, and for sortByKey key order inside a bin.
   ascending order and binByKey reports num_data bins of one key each.
 * Random keys over narrow, negative and full int32 ranges, sub-ranges
   [begin, end), one bin, equal keys, a single key and an empty range.
+* permute of int32 / int64 members (moved bit for bit with the rest).
 """
 import numpy as np
 import pytest
@@ -97,3 +98,26 @@ def test_single_key_and_empty_range(oracle):
     keys = torch.arange(10, dtype=torch.int32, device="cuda")
     bd = C.binByKey(keys, 4, 6, 6)
     assert bd.numBin() == 5 and int(bd.counts.sum()) == 0 and int(bd.offsets.abs().sum()) == 0
+
+
+def test_permute_moves_integer_members_bit_for_bit():
+    """The reference permutes whole AoSoAs, int members included
+    (tstSort.hpp's int member): int32 and int64 fields move bit for bit,
+    including patterns that read as NaNs when taken as floats."""
+    rng = np.random.default_rng(21)
+    n = 5000
+    keys = rng.integers(0, 300, size=n).astype(np.int32)
+    ids32 = rng.integers(-2**31, 2**31 - 1, size=(n, 2), endpoint=True).astype(np.int32)
+    ids32[200:204, 0] = [0x7FC00001, -1, 0x7F800001, -0x7FFFFFFF]  # inside the permuted range
+    ids64 = rng.integers(-2**63, 2**63 - 1, size=n, endpoint=True, dtype=np.int64)
+    ids64[200:203] = [0x7FF0000000000001, -1, 0x7FF8000000000123]
+    t32 = torch.tensor(ids32, device="cuda")
+    t64 = torch.tensor(ids64, device="cuda")
+    bd = C.binByKey(torch.tensor(keys, device="cuda"), 299, 100, 4900)
+    C.permute(bd, t32, t64)
+    perm = bd.permutes.cpu().numpy()
+    r32, r64 = ids32.copy(), ids64.copy()
+    r32[100:4900] = ids32[perm]
+    r64[100:4900] = ids64[perm]
+    assert np.array_equal(t32.cpu().numpy(), r32)
+    assert np.array_equal(t64.cpu().numpy(), r64)
