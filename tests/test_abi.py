@@ -114,3 +114,6 @@ def test_argument_checks_fail_loudly(lib):
                                       None)
     assert st == L.CGX_ERR_INVALID_ARG
     assert b"handle" in lib.cgx_last_error()
+    # binByKey / sortByKey: the handle is checked first, then the range and nbin
+    st = lib.cgx_bin_by_key_range(None, None, 0, 4, 3, 0, None, None, None, None)
+    assert st == L.CGX_ERR_INVALID_ARG and b"handle" in lib.cgx_last_error()
