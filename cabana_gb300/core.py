@@ -53,31 +53,43 @@ class LinkedCellList:
         nd = len(grid_min)
         if nd not in (2, 3) or len(grid_max) != nd or len(grid_delta) != nd:
             raise ValueError("grid_min / grid_max / grid_delta need 2 or 3 entries each")
-        n = positions.size if isinstance(positions, Slice) else positions.shape[0]
-        end = n if end is None else end
         d3 = ctypes.c_double * 3
         nb = (ctypes.c_int32 * 3)()
         # bin counts: a 2D grid is counted as a 3D one with a single z cell
         pad = lambda v, fill: d3(*(list(v) + [fill] * (3 - nd)))  # noqa: E731
         self._min, self._max, self._delta = pad(grid_min, 0.0), pad(grid_max, 1.0), pad(grid_delta, 1.0)
+        d2 = ctypes.c_double * 2
+        self._grid2 = (d2(*grid_min), d2(*grid_max), d2(*grid_delta)) if nd == 2 else None
         L.check(L.lib().cgx_cartesian_num_bins(self._min, self._max, self._delta, nb))
         self._nbin = tuple(nb)[:nd]
+        self._handle, self._stream = handle, stream
+        self._sorted = False
+        self.build(positions, begin, end)
+
+    def build(self, positions, begin=0, end=None):
+        """Rebin (LinkedCellList::build, Cabana_LinkedCellList.hpp:651-775):
+        the grid stays, the particles [begin, end) of `positions` are binned
+        again, and the list counts as not sorted."""
+        n = positions.size if isinstance(positions, Slice) else positions.shape[0]
+        end = n if end is None else end
+        if not 0 <= begin <= end <= n:
+            raise ValueError("need 0 <= begin <= end <= number of positions")
         total = self.totalBins()
         dev = positions.storage.device if isinstance(positions, Slice) else positions.device
         counts = torch.zeros(total, dtype=torch.int32, device=dev)
         offsets = torch.zeros(total, dtype=torch.int64, device=dev)
         permutes = torch.zeros(max(1, end - begin), dtype=torch.int64, device=dev)
-        h = handle or L.default_handle()
+        h = self._handle or L.default_handle()
         outs = (ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(offsets.data_ptr()),
-                ctypes.c_void_p(permutes.data_ptr()), _stream(stream))
+                ctypes.c_void_p(permutes.data_ptr()), _stream(self._stream))
         desc = ctypes.byref(field_descriptor(positions))
-        if nd == 3:
+        if self._grid2 is None:
             L.check(L.lib().cgx_linked_cell_build(h.ptr, desc, begin, end, self._min, self._max, self._delta, *outs))
         else:
-            d2 = ctypes.c_double * 2
-            L.check(L.lib().cgx_linked_cell_build_2d(h.ptr, desc, begin, end, d2(*grid_min), d2(*grid_max),
-                                                     d2(*grid_delta), *outs))
+            L.check(L.lib().cgx_linked_cell_build_2d(h.ptr, desc, begin, end, *self._grid2, *outs))
         self._data = BinningData(begin, end, counts, offsets, permutes[: end - begin])
+        self._sorted = False
+        self._particle_bins = None  # formed on first use (storeParticleBins)
 
     def numBin(self, d):
         return self._nbin[d]
@@ -115,6 +127,63 @@ class LinkedCellList:
 
     def binningData(self):
         return self._data
+
+    def ijkBinIndex(self, cardinal):
+        """The (i, j[, k]) of a cardinal bin index (k, then j, fastest)."""
+        out = []
+        for d in range(len(self._nbin) - 1, -1, -1):
+            out.append(cardinal % self._nbin[d])
+            cardinal //= self._nbin[d]
+        return tuple(reversed(out))
+
+    def numParticles(self):
+        return self._data.end - self._data.begin
+
+    def getParticleBegin(self):
+        return self._data.begin
+
+    def getParticleEnd(self):
+        return self._data.end
+
+    def rangeBegin(self):
+        return self._data.begin
+
+    def rangeEnd(self):
+        return self._data.end
+
+    def update(self, sorted):
+        """Record whether the particles have been permuted into bin order
+        (LinkedCellList::update); the per-particle bins follow."""
+        self._sorted = bool(sorted)
+        self._particle_bins = None
+
+    def sorted(self):
+        return self._sorted
+
+    def storeParticleBins(self):
+        """The bin of every binned particle (LinkedCellList::storeParticleBins,
+        Cabana_LinkedCellList.hpp:778-787 and :800-823): indexed by the
+        particle's position in bin order once sorted, else by its original
+        index, both relative to begin."""
+        d = self._data
+        n = d.end - d.begin
+        cells = torch.arange(d.counts.numel(), dtype=torch.int32, device=d.counts.device)
+        in_order = torch.repeat_interleave(cells, d.counts.to(torch.int64), output_size=n)
+        if self._sorted:
+            self._particle_bins = in_order
+        else:
+            bins = torch.empty(n, dtype=torch.int32, device=d.counts.device)
+            bins[d.permutes - d.begin] = in_order
+            self._particle_bins = bins
+        return self._particle_bins
+
+    def getParticleBins(self):
+        return self._particle_bins if self._particle_bins is not None else self.storeParticleBins()
+
+    def getParticleBin(self, particle_index):
+        if not self._data.begin <= particle_index < self._data.end:
+            raise IndexError("particle outside the binned range")
+        return int(self.getParticleBins()[particle_index - self._data.begin])
 
 
 def createLinkedCellList(positions, grid_delta, grid_min, grid_max, begin=0, end=None, **kw):
@@ -195,6 +264,10 @@ def permute(binning, *fields, handle=None, stream=None):
     """In-place permute of every field over the binning's range (float32,
     float64, int32 or int64 tensors, or Slices)."""
     data = binning.binningData() if isinstance(binning, LinkedCellList) else binning
+    if isinstance(binning, LinkedCellList):
+        # permute(LinkedCellList&, ...) marks the list sorted
+        # (Cabana_LinkedCellList.hpp:1130-1146)
+        binning.update(True)
     if data.end == data.begin or not fields:
         return
     n = len(fields)
