@@ -196,7 +196,21 @@ def _int_keys(keys):
     return keys.to(torch.int32).contiguous()
 
 
+def _slice_keys(s):
+    """The values of a rank-1 Slice as a contiguous tensor (the reference
+    copies a key slice into a View first, copySliceToView,
+    core/src/Cabana_Sort.hpp:459-545): element i sits at offset +
+    soa_stride * (i / VL) + i % VL of the storage."""
+    if s.comps != 1:
+        raise ValueError("key slices must have one component per particle")
+    i = torch.arange(s.size, device=s.storage.device)
+    idx = s.offset + (i // s.vector_length) * s.soa_stride + i % s.vector_length
+    return s.storage.reshape(-1)[idx]
+
+
 def _bin_range(keys, nbin, begin, end, sort_within_bins, handle, stream):
+    if isinstance(keys, Slice):
+        keys = _slice_keys(keys)
     end = keys.shape[0] if end is None else end
     if nbin < 0:
         raise ValueError("nbin must be >= 0")
@@ -215,15 +229,18 @@ def _bin_range(keys, nbin, begin, end, sort_within_bins, handle, stream):
 def binByKey(keys, nbin, begin=0, end=None, handle=None, stream=None):
     """Cabana::binByKey (core/src/Cabana_Sort.hpp:411-443): nbin + 1 bins
     splitting [min, max] of keys[begin, end) evenly (Kokkos::BinOp1D; one key
-    value per bin when max - min <= nbin); stable order inside a bin."""
+    value per bin when max - min <= nbin); stable order inside a bin. `keys`
+    is an integer tensor or a rank-1 Slice of an integer member."""
     return _bin_range(keys, nbin, begin, end, False, handle, stream)
 
 
 def sortByKey(keys, begin=0, end=None, handle=None, stream=None):
     """Cabana::sortByKey (core/src/Cabana_Sort.hpp:364-393): BinOp1D bins with
     nbin = (end - begin) // 2, entries ordered by key inside each bin (so the
-    permutation sorts by key; equal keys keep index order)."""
-    end = keys.shape[0] if end is None else end
+    permutation sorts by key; equal keys keep index order). `keys` is an
+    integer tensor or a rank-1 Slice of an integer member."""
+    if end is None:
+        end = keys.size if isinstance(keys, Slice) else keys.shape[0]
     return _bin_range(keys, (end - begin) // 2, begin, end, True, handle, stream)
 
 

@@ -112,3 +112,43 @@ def test_ijk_bin_index_round_trip(fake, oracle):
     assert lcl.ijkBinIndex(4 * 6 * 8 - 1) == (3, 5, 7)
     for c in range(0, 4 * 6 * 8, 7):
         assert lcl.cardinalBinIndex(lcl.ijkBinIndex(c)) == c
+
+
+class _FakeSortLib(_FakeLib):
+    """cgx_bin_by_key_range from the oracle, reading the keys the mirror passes."""
+
+    def cgx_bin_by_key_range(self, h, keys_p, begin, end, nbin, sort_within, counts_p, offsets_p, permutes_p,
+                             stream):
+        n = end
+        keys = np.ctypeslib.as_array(ctypes.cast(keys_p.value, ctypes.POINTER(ctypes.c_int32)), shape=(n,)).copy()
+        self.keys_seen = keys
+        counts, offsets, permutes = self.oracle.bin_by_key_range(keys, nbin, begin, end, bool(sort_within))
+        for arr, ptr in ((counts, counts_p), (offsets, offsets_p), (permutes, permutes_p)):
+            ctypes.memmove(ptr.value, arr.ctypes.data, arr.nbytes)
+        return 0
+
+
+def test_sort_and_bin_by_key_slice(monkeypatch, oracle):
+    """tstSort.hpp:202-420 (sortByKey / binByKey of a slice): keys taken from
+    an int member of an AoSoA (vector length 8, two int members per SoA)."""
+    lib = _FakeSortLib(oracle, None)
+    monkeypatch.setattr(L, "lib", lambda: lib)
+    monkeypatch.setattr(L, "default_handle", lambda: types.SimpleNamespace(ptr=None))
+    monkeypatch.setattr(C, "_stream", lambda s: ctypes.c_void_p(0))
+    n, vl = 100, 8
+    nsoa = (n + vl - 1) // vl
+    storage = torch.full((nsoa * 2 * vl,), -7, dtype=torch.int32)
+    rev = torch.arange(n - 1, -1, -1, dtype=torch.int32)
+    i = torch.arange(n)
+    storage[(i // vl) * 2 * vl + vl + i % vl] = rev  # member 1: keys(p) = reverse index
+    keys = C.Slice(storage, vl, vl, 2 * vl, 1, n)
+    bd = C.sortByKey(keys)
+    assert np.array_equal(lib.keys_seen, rev.numpy())
+    assert np.array_equal(bd.permutes.numpy(), np.arange(n - 1, -1, -1))
+    bd = C.binByKey(keys, n - 1)
+    assert bd.numBin() == n and (bd.counts.numpy() == 1).all()
+    assert np.array_equal(bd.offsets.numpy(), np.arange(n))
+    with pytest.raises(ValueError):
+        C.binByKey(C.Slice(storage, 0, vl, 2 * vl, 2, n), 4)
+    with pytest.raises(TypeError):
+        C.binByKey(torch.zeros(5), 4)
