@@ -270,10 +270,14 @@ def _move_descriptor(f):
     tensor travels as the float type of its element size (int32 as float32,
     int64 as float64), as the reference permutes int members with the rest of
     the AoSoA."""
-    if isinstance(f, torch.Tensor) and not f.dtype.is_floating_point:
-        if f.dtype == torch.bool or f.element_size() not in (4, 8):
-            raise TypeError(f"permute moves 4- or 8-byte elements; got {f.dtype}")
-        return field_descriptor(f.view(torch.float32 if f.element_size() == 4 else torch.float64))
+    t = f.storage if isinstance(f, Slice) else f
+    if isinstance(t, torch.Tensor) and not t.dtype.is_floating_point:
+        if t.dtype == torch.bool or t.element_size() not in (4, 8):
+            raise TypeError(f"permute moves 4- or 8-byte elements; got {t.dtype}")
+        as_float = t.view(torch.float32 if t.element_size() == 4 else torch.float64)
+        if isinstance(f, Slice):
+            return Slice(as_float, f.offset, f.vector_length, f.soa_stride, f.comps, f.size).descriptor()
+        return field_descriptor(as_float)
     return field_descriptor(f)
 
 

@@ -152,3 +152,16 @@ def test_sort_and_bin_by_key_slice(monkeypatch, oracle):
         C.binByKey(C.Slice(storage, 0, vl, 2 * vl, 2, n), 4)
     with pytest.raises(TypeError):
         C.binByKey(torch.zeros(5), 4)
+
+
+def test_permute_descriptor_of_integer_members():
+    """Integer members travel as the float type of their size (permute moves
+    bits), for tensors and for Slices of an AoSoA's int storage."""
+    storage = torch.zeros(64, dtype=torch.int32)
+    d = C._move_descriptor(C.Slice(storage, 8, 8, 16, 1, 30))
+    assert d.dtype == L.CGX_F32 and d.data == storage.data_ptr() + 8 * 4
+    assert (d.vector_length, d.soa_stride, d.comp_stride) == (8, 16, 8)
+    d = C._move_descriptor(C.Slice(torch.zeros(32, dtype=torch.int64), 0, 4, 8, 2, 12))
+    assert d.dtype == L.CGX_F64
+    with pytest.raises(TypeError):
+        C._move_descriptor(C.Slice(torch.zeros(32, dtype=torch.int16), 0, 4, 8, 1, 12))
