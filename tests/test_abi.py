@@ -117,3 +117,11 @@ def test_argument_checks_fail_loudly(lib):
     # binByKey / sortByKey: the handle is checked first, then the range and nbin
     st = lib.cgx_bin_by_key_range(None, None, 0, 4, 3, 0, None, None, None, None)
     assert st == L.CGX_ERR_INVALID_ARG and b"handle" in lib.cgx_last_error()
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without libcgx.so every entry point refuses to run."""
+    monkeypatch.setattr(L, "_lib", None)
+    monkeypatch.setattr(L, "LIB_PATH", str(tmp_path / "libcgx.so"))
+    with pytest.raises(RuntimeError, match="missing"):
+        L.lib()
